@@ -1,0 +1,315 @@
+"""Benchmark of the GB300 FDTD stepper (one JSON line on rank 0).
+
+Workload (default "sweep"): the batched CEP/amplitude sweep — 96 junction
+instances on uneven grids (32 x 96^3, 32 x 128^3, 32 x 192^3), FP32 fields,
+one launch per time step over all instances.  A bench step is one FDTD time
+step of the whole batch.  The metric is voxel-steps/s = sum of instance
+voxels x steps / device time.  Also reported: the plain FP64 path on a grid
+whose state is well above L2 (512 x 512 x 384), its roofline fraction, and
+the FP32/FP64 gap-field error.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload sweep|bowtie|junction] [--schedule fused|split]
+
+Under torchrun each rank runs its own full batch (weak scaling, no
+collective on the data path); value = all ranks' voxel-steps / max time.
+`--impl reference` times the CPU restatement (the reference's stepper,
+meep, cannot run here) on the host cores with a bounded sample per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-steps/s & %HBM peak: FP32 batched vs FP64 plain at <=1e-4 rel gap-field err"
+UNIT = "voxel-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="sweep", choices=["sweep", "bowtie", "junction"])
+    p.add_argument("--schedule", default="fused", choices=["fused", "split"])
+    p.add_argument("--e2e-steps", type=int, default=400)
+    p.add_argument("--no-extras", action="store_true", help="skip the FP64 and error legs")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_instances(name, rank=0):
+    from sim_juncs_gb300 import configs
+    if name == "sweep":
+        return configs.sweep_instances(seed=rank), {
+            "workload": "cep_amplitude_sweep", "instances": 96,
+            "grids": "32x96^3 + 32x128^3 + 32x192^3", "px_per_um": [30, 40, 60],
+            "cell_um": 3.2, "pml_um": 0.5, "steps_per_run": 4000, "seed": rank}
+    if name == "bowtie":
+        return [configs.bowtie_instance()], {"workload": "bowtie", "grid": "512x512x384",
+                                             "px_per_um": 40, "pml_um": 1.0, "steps_per_run": 20000}
+    return [configs.junction_instance()], {"workload": "junction", "grid": "64^3", "px_per_um": 20,
+                                           "pml_um": 0.5, "steps_per_run": 2000}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def time_steps(f, torch, steps, warmup, launches_per_step):
+    """Device time of `steps` steps on f's stream (CUDA events), after warmup."""
+    f.step(warmup)
+    f.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if torch.distributed.is_initialized():
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    f.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return ms / 1000.0, steps * launches_per_step
+
+
+def run_ours(args):
+    import torch
+    from sim_juncs_gb300 import build
+    from sim_juncs_gb300.fields import Fields
+    from sim_juncs_gb300 import configs
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    # a real (non-legacy) stream shared by torch's events and the library
+    torch.cuda.set_stream(torch.cuda.Stream())
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    if rank == 0:
+        build.build()
+    if ws > 1:
+        torch.distributed.barrier()
+
+    insts, cfg = workload_instances(args.workload, rank)
+    f = Fields(insts, "f32", args.schedule, stream=torch.cuda.current_stream())
+    has_probes = any(i.probes for i in insts)
+    lps = (1 if args.schedule == "fused" else 2) + (1 if has_probes and args.schedule == "split" else 0)
+    voxels = f.voxels()
+    bytes_step = f.bytes_per_step()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    secs, launches = time_steps(f, torch, args.steps, args.warmup, lps)
+    clk = clocks.stop()
+    t = torch.tensor([secs], device="cuda")
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    secs = float(t.item())
+    value = voxels * args.steps * ws / secs
+    peak, peak_kind = measured_peak()
+    achieved = bytes_step / (secs / args.steps) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(cfg, schedule=args.schedule, l2="state larger than L2 (no flush needed)",
+                       voxels_per_step=voxels, parallelism=f"replicas{ws}"),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": bytes_step,
+                     "kernel": "fused stepper" if args.schedule == "fused" else "split H+E stepper"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    f.close()
+    del f
+
+    if rank == 0 and not args.no_extras:
+        out["fp64_plain"] = fp64_leg(torch, args)
+        out["fp32_vs_fp64"] = error_leg(args)
+    if rank == 0:
+        out["e2e"] = e2e_leg(torch, args, insts)
+        out["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def fp64_leg(torch, args):
+    """Plain FP64 path on the 512 x 512 x 384 bowtie grid (state >> L2)."""
+    from sim_juncs_gb300 import configs
+    from sim_juncs_gb300.fields import Fields
+    inst = configs.bowtie_instance()
+    f = Fields(inst, "f64", args.schedule, stream=torch.cuda.current_stream())
+    steps = max(5, args.steps // 4)
+    secs, _ = time_steps(f, torch, steps, 3, 1)
+    peak, kind = measured_peak()
+    b = f.bytes_per_step()
+    ach = b / (secs / steps) / 1e9
+    res = {"workload": "bowtie 512x512x384 f64", "value": inst.grid.voxels * steps / secs, "unit": UNIT,
+           "ms_per_step": secs / steps * 1e3, "steps": steps,
+           "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                        "peak_kind": kind, "algorithmic_bytes_per_step": b}}
+    f.close()
+    return res
+
+
+def error_leg(args):
+    """FP32 vs FP64 relative gap-field error on the 64^3 junction (2000 steps)."""
+    from sim_juncs_gb300 import configs
+    from sim_juncs_gb300.fields import Fields
+    inst = configs.junction_instance()
+    a = Fields(inst, "f64", args.schedule)
+    b = Fields(inst, "f32", args.schedule)
+    a.step(2000)
+    b.step(2000)
+    m64, m32 = a.monitors()[:4], b.monitors()[:4]
+    d64, d32 = a.dft()[:4], b.dft()[:4]
+    return {"workload": "junction 64^3, 2000 steps, Ex at 4 gap points",
+            "monitor_rel_err": float(np.max(np.abs(m32 - m64)) / np.max(np.abs(m64))),
+            "dft_rel_err": float(np.max(np.abs(d32 - d64)) / np.max(np.abs(d64)))}
+
+
+def e2e_leg(torch, args, insts):
+    """Whole job through the C ABI from host descriptors: create (uploads the
+    scene, rasterises on the device), e2e_steps steps (source tables go H2D),
+    then monitors + DFT back to host buffers.  Wall clock, host to host."""
+    from sim_juncs_gb300.fields import Fields
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f = Fields(insts, "f32", args.schedule)
+    f.step(args.e2e_steps)
+    outs = [(f.monitors(q), f.dft(q)) for q in range(f.n_instances)]
+    t1 = time.perf_counter()
+    voxels = f.voxels()
+    h2d, d2h = f.transfer_bytes()
+    f.close()
+    return {"value": voxels * args.e2e_steps / (t1 - t0), "unit": UNIT,
+            "steps": args.e2e_steps, "seconds": t1 - t0,
+            "h2d_bytes_per_step": h2d / args.e2e_steps, "d2h_bytes_per_step": d2h / args.e2e_steps,
+            "includes": "create + device rasterise + steps + monitor/DFT read-back"}
+
+
+def cpu_sample():
+    """Bounded CPU sample: one 96^3 sweep member, FP64 restatement."""
+    from sim_juncs_gb300 import configs
+    return configs.junction_instance(n=96, res=30.0, probe_components=("Ez",), dft=False)
+
+
+def cpu_baseline(args, steps=60):
+    from oracle import oracle
+    oracle.build()
+    inst = cpu_sample()
+    o = oracle.OracleFields(inst)
+    o.step(2)
+    t0 = time.perf_counter()
+    o.step(steps)
+    secs = time.perf_counter() - t0
+    return {"value": inst.grid.voxels * steps / secs, "unit": UNIT, "cores": os.cpu_count(),
+            "kind": "port", "sample": f"one 96^3 sweep member, {steps} FP64 steps (OpenMP restatement; "
+                                       "meep v1.24 is not available to run)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    inst = cpu_sample()
+    o = oracle.OracleFields(inst)
+    per = 10
+    for _ in range(args.warmup):
+        o.step(per)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(per)
+    secs = time.perf_counter() - t0
+    value = inst.grid.voxels * per * args.steps / secs
+    _, cfg = workload_instances(args.workload)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference", "config": cfg,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"{per} FP64 steps of one 96^3 sweep member per bench step "
+                                      "(CPU restatement; meep v1.24 is not available to run)"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

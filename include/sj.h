@@ -1,0 +1,314 @@
+/*
+ * sj.h — C ABI of the sim_juncs GB300 FDTD stepper.
+ *
+ * This library replaces the meep::fields object that sim_juncs' bound_geom
+ * owns (src/disp.hpp:175-177) and the time loop that drives it
+ * (bound_geom::run, src/disp.cpp:690-749).  Every entry point below names the
+ * reference call it stands in for.
+ *
+ * Conventions
+ *   - plain C, no exceptions cross the ABI; every call returns an int status:
+ *     0 = success, negative = error (SJ_E_*), with a message from
+ *     sj_last_error(sim) (or sj_last_error(NULL) after a failed create);
+ *   - device memory is owned by the library, host arrays by the caller;
+ *   - units are meep units: lengths in "a" (= 1/um_scale um), c = 1,
+ *     frequencies in c/a, times in a/c;
+ *   - field arrays exchanged with the host are [nz][ny][nx], x fastest.
+ *
+ * Discretisation (the definition the CPU oracle and the kernels share)
+ *   Integer Yee point (i,j,k) sits at origin + (i,j,k)*dx.  Component
+ *   offsets, in units of dx: Ex(1/2,0,0) Ey(0,1/2,0) Ez(0,0,1/2)
+ *   Hx(0,1/2,1/2) Hy(1/2,0,1/2) Hz(1/2,1/2,0).  Values outside the
+ *   nx*ny*nz arrays are zero.  mu = 1, so B = H and no B array exists.
+ *   One step n -> n+1 (S = dt/dx):
+ *     H^{n+1/2} = H^{n-1/2} - S*curl_fwd(E^n) [+ CPML psi] - dt*M
+ *     P_p^{n+1} = A_p P_p^n + B_p P_p^{n-1} + C_p sigma_p E^n
+ *     E^{n+1}   = E^n + eps_inf^{-1} ( S*curl_bwd(H^{n+1/2}) [+ CPML psi]
+ *                                     - dt*J^{n+1/2} - sum_p (P_p^{n+1}-P_p^n) )
+ *   with meep's Lorentzian form A_p = (2 - w^2 dt^2 L)/(1+g dt/2),
+ *   B_p = -(1 - g dt/2)/(1+g dt/2), C_p = w^2 dt^2/(1+g dt/2),
+ *   w = 2 pi omega_0, g = 2 pi gamma, L = 0 for Drude (no omega_0
+ *   denominator) and 1 for Lorentz.  Monitors sample E^n before step n when
+ *   n % save_span == 0 (src/disp.cpp:721); DFT sums accumulate
+ *   dt * F(t) * exp(+i 2 pi f t) over every step, t = n dt for E probes and
+ *   (n - 1/2) dt for H probes.
+ */
+#ifndef SJ_H
+#define SJ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SJ_ABI_VERSION 1
+
+/* status codes */
+#define SJ_OK 0
+#define SJ_E_INVALID (-1)   /* bad argument or descriptor */
+#define SJ_E_CUDA (-2)      /* a CUDA runtime/driver call failed */
+#define SJ_E_NOMEM (-3)     /* device or host allocation failed */
+#define SJ_E_RANGE (-4)     /* index / capacity out of range */
+#define SJ_E_DIVERGED (-5)  /* field exceeded the divergence guard */
+#define SJ_E_TIMEOUT (-6)   /* a bounded device wait gave up */
+
+/* field components, same order as meep's Ex..Hz (src/disp.cpp:334-344) */
+enum { SJ_EX = 0, SJ_EY = 1, SJ_EZ = 2, SJ_HX = 3, SJ_HY = 4, SJ_HZ = 5 };
+
+/* precision of fields, polarisations and CPML auxiliaries; DFT and
+   monitor sums are always FP64 */
+enum { SJ_F64 = 0, SJ_F32 = 1 };
+
+/* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel, SPLIT the
+   two-pass (H then E) reference schedule kept for cross-checking */
+enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1 };
+
+#define SJ_MAX_POLES 8
+#define SJ_MAX_SOURCES 4
+#define SJ_MAX_REGIONS 8
+#define SJ_MAX_CSG_NODES 256
+
+/* ---------------------------------------------------------------- grid */
+/* meep::vol3d(L, L, L, res) built in structure_from_settings
+   (src/disp.cpp:505-510); nx = grid_num from correct_defaults
+   (src/argparse.h:171-191), dx = 1/resolution.  dt <= 0 selects
+   meep's default Courant factor 0.5 (dt = dx/2). */
+typedef struct {
+    int32_t nx, ny, nz;
+    double dx;
+    double dt;
+    double origin[3];
+} sj_grid_desc;
+
+/* ---------------------------------------------------------------- materials */
+/* one meep::lorentzian_susceptibility (src/disp.cpp:538-547): omega_0 and
+   gamma already divided by um_scale, drude != 0 for no_omega_0_denominator */
+typedef struct {
+    double omega_0;
+    double gamma;
+    int32_t drude;
+    int32_t _pad;
+} sj_pole;
+
+/* Flattened CSG program of one root composite_object, in postfix order:
+   leaves push in(r) (0/1), composites pop two and push the combination.
+   Mirrors composite_object::in and the primitives' in()
+   (src/cgs.cpp:34-120, 403-449), in the same floating-point operation
+   order (matrix rows summed left to right, no fused multiply-add).
+     leaf point   r' = m * r             (m = product of the ancestors'
+                                          trans_mat; exact when they are
+                                          identities, as in every shipped
+                                          junction file)
+                  q  = t * (r' - c)      (t = the primitive's own trans_mat)
+     SJ_CSG_BOX      |q_a| > p[a] for any a      -> invert, else 1-invert
+     SJ_CSG_SPHERE   |q| > p[0]                  -> invert, else 1-invert
+     SJ_CSG_CYLINDER q_z<0 || q_z>p[0] || (qx^2+qy^2)*p[0] > (p[2]-p[1])*q_z + p[1]*p[0]
+                                                 -> invert, else 1-invert
+                     (p[0] = height, p[1] = r1^2, p[2] = r2^2)
+     SJ_CSG_PLANE    dot(r', p[0..2]) > p[3] -> 0 else 1
+                     (plane::in ignores invert and its own trans_mat)
+     SJ_CSG_UNION / SJ_CSG_INTERSECT   pop b, pop a, push invert ^ (a|b) / (a&b)
+     SJ_CSG_PASS     pop a, push invert ^ a     (composite with one child)
+     SJ_CSG_CONST    push invert                (composite with no child)
+     SJ_CSG_NOOP     push 0                     (CGS_CMB_NOOP)
+   Difference is emitted as INTERSECT with the right child's invert set, as
+   composite_object::add_child does. */
+enum {
+    SJ_CSG_BOX = 0, SJ_CSG_SPHERE = 1, SJ_CSG_CYLINDER = 2, SJ_CSG_PLANE = 3,
+    SJ_CSG_UNION = 4, SJ_CSG_INTERSECT = 5, SJ_CSG_PASS = 6, SJ_CSG_CONST = 7,
+    SJ_CSG_NOOP = 8
+};
+typedef struct {
+    int32_t op;
+    int32_t invert;
+    double m[9];   /* row-major 3x3, ancestors' transform */
+    double t[9];   /* row-major 3x3, primitive's own transform */
+    double c[3];
+    double p[4];
+} sj_csg_node;
+
+/* one root of the scene: the region_scale_pair of cgs_material_function
+   (src/disp.hpp:44-47) plus the root's susceptibilities */
+typedef struct {
+    int32_t n_nodes;
+    const sj_csg_node* nodes;
+    double eps;                 /* the root's "eps" metadata (scale s) */
+    int32_t n_poles;
+    const sj_pole* poles;       /* meep units */
+    const double* sigma;        /* [n_poles], already divided by thickness */
+} sj_region_desc;
+
+/* cgs_material_function semantics (src/disp.cpp:264-283) with smooth_n = 0.
+   SJ_EPS_SUM (the reference's behaviour):
+     eps(r) = sum_roots [ambient + (s_root - ambient) * in_root(r)]
+     (ambient alone when there is no root), so empty space carries
+     n_roots * ambient;
+   SJ_EPS_FIRST (what the comment at src/disp.cpp:271 describes):
+     eps(r) = s of the first root containing r, else ambient.
+   In both modes sigma_{root,q}(r) = sigma * in_root(r), except that under
+   SJ_EPS_FIRST only the first containing root contributes poles. */
+enum { SJ_EPS_SUM = 0, SJ_EPS_FIRST = 1 };
+typedef struct {
+    double ambient_eps;
+    int32_t n_regions;
+    int32_t combine;            /* SJ_EPS_SUM (default) or SJ_EPS_FIRST */
+    const sj_region_desc* regions;
+} sj_scene_desc;
+
+/* Material description: either an explicit per-component class map with a
+   class table, or a scene rasterised on the device (class = bitmask of the
+   regions containing the component's Yee point). */
+typedef struct {
+    /* explicit form (used when class_map != NULL) */
+    int32_t n_classes;          /* <= 255 */
+    const double* eps_inf;      /* [n_classes] */
+    int32_t n_poles;            /* <= SJ_MAX_POLES */
+    const sj_pole* poles;       /* [n_poles] */
+    const double* sigma;        /* [n_classes][n_poles] */
+    const uint8_t* class_map;   /* [3][nz][ny][nx]: class at Ex, Ey, Ez points */
+    /* scene form (used when class_map == NULL) */
+    const sj_scene_desc* scene;
+} sj_material_desc;
+
+/* ---------------------------------------------------------------- PML */
+/* meep::pml(thickness) (src/disp.cpp:527): stretched-coordinate absorber on
+   every face.  sigma(u) = sigma_max (u/d)^power, sigma_max chosen so the
+   round-trip reflection at normal incidence is r_asymptotic. */
+typedef struct {
+    double thickness[3][2];     /* [axis][low, high] in length units */
+    double r_asymptotic;        /* <= 0 -> 1e-15 (meep's default) */
+    double power;               /* <= 0 -> 2 (meep's quadratic profile) */
+    double alpha;               /* CFS frequency shift, 0 = none */
+} sj_pml_desc;
+
+/* ---------------------------------------------------------------- sources */
+/* source_info + gaussian_src_time_phase / continuous_src_time as passed to
+   fields.add_volume_source (src/disp.cpp:595-620).  Times and frequency in
+   meep units (the fs -> meep conversion of src/disp.cpp:604-609 is the
+   caller's, as in the reference).  The current density injected is
+   Re[amplitude * (d(t) - d(t - dt)) / dt] * weight(r), d the dipole
+   function, evaluated at t = (n + 1/2) dt for E-components and n dt for H. */
+enum { SJ_SRC_GAUSSIAN = 0, SJ_SRC_CONTINUOUS = 1 };
+typedef struct {
+    int32_t component;
+    int32_t kind;
+    double frequency;
+    double width;
+    double phase;
+    double start_time;
+    double end_time;
+    double amplitude[2];        /* complex (re, im) */
+    double lo[3], hi[3];        /* source volume; zero extent -> sheet */
+} sj_source_desc;
+
+/* ---------------------------------------------------------------- probes */
+/* fields.get_field(component, loc) at monitor points (src/disp.cpp:724),
+   trilinear interpolation between the component's Yee points. */
+enum { SJ_PROBE_MONITOR = 1, SJ_PROBE_DFT = 2 };
+typedef struct {
+    int32_t component;
+    int32_t flags;              /* SJ_PROBE_MONITOR | SJ_PROBE_DFT */
+    double pos[3];
+} sj_probe_desc;
+
+/* one simulation instance (one bound_geom) */
+typedef struct {
+    sj_grid_desc grid;
+    sj_material_desc material;
+    sj_pml_desc pml;
+    int32_t n_sources;
+    const sj_source_desc* sources;
+    int32_t n_probes;
+    const sj_probe_desc* probes;
+    int32_t n_freqs;
+    const double* freqs;        /* DFT frequencies (meep units) */
+    int32_t save_span;          /* monitor sampling period (>= 1) */
+} sj_instance_desc;
+
+typedef struct sj_sim sj_sim;
+
+/* ---------------------------------------------------------------- lifecycle */
+int sj_abi_version(void);
+/* sizeof of the descriptor structs above, in declaration order
+   (0 = sj_grid_desc ... 9 = sj_instance_desc); -1 for an unknown index */
+int64_t sj_abi_struct_size(int32_t which);
+const char* sj_last_error(const sj_sim* sim);
+
+/* fields(strct) + add_volume_source + parse_monitors
+   (src/disp.cpp:557-645): builds one instance on the current device. */
+int sj_create(const sj_instance_desc* inst, int32_t precision, sj_sim** out);
+
+/* many independent instances stepped by one launch per step (batched
+   CEP/amplitude sweeps); instance i keeps its own grid, materials, PML,
+   sources and probes. */
+int sj_batch_create(int32_t n_instances, const sj_instance_desc* insts,
+                    int32_t precision, sj_sim** out);
+
+/* ~bound_geom / ~fields (src/disp.cpp:647-649) */
+int sj_destroy(sj_sim* sim);
+
+/* stream used by every later call (a cudaStream_t); NULL = the library's own */
+int sj_set_stream(sj_sim* sim, void* cuda_stream);
+int sj_set_schedule(sj_sim* sim, int32_t schedule);
+int sj_synchronize(sj_sim* sim);
+
+/* ---------------------------------------------------------------- stepping */
+/* n_steps iterations of the loop body at src/disp.cpp:719-741: sample
+   monitors when step % save_span == 0, accumulate DFTs, then fields.step().
+   Asynchronous on the sim's stream. */
+int sj_step(sj_sim* sim, int64_t n_steps);
+
+/* same, recorded once into a CUDA graph of `chunk` steps and replayed */
+int sj_step_graph(sj_sim* sim, int64_t n_steps, int32_t chunk);
+
+/* ---------------------------------------------------------------- queries */
+int64_t sj_steps_done(const sj_sim* sim);
+int32_t sj_n_instances(const sj_sim* sim);
+/* fields.time() (src/disp.cpp:733) and fields.dt (src/disp.cpp:704) */
+double sj_time(const sj_sim* sim, int32_t inst);
+double sj_dt(const sj_sim* sim, int32_t inst);
+/* fields.last_source_time() (src/disp.cpp:625) */
+double sj_last_source_time(const sj_sim* sim, int32_t inst);
+/* number of monitor samples taken so far (ceil(steps / save_span)) */
+int64_t sj_n_samples(const sj_sim* sim, int32_t inst);
+/* bytes this sim has copied host->device and device->host so far */
+int sj_transfer_bytes(const sj_sim* sim, int64_t* h2d, int64_t* d2h);
+/* per-instance voxel count and algorithmic bytes per step (roofline model) */
+int64_t sj_voxels(const sj_sim* sim, int32_t inst);
+double sj_bytes_per_step(const sj_sim* sim, int32_t inst);
+
+/* ---------------------------------------------------------------- read-back */
+/* field_times (src/disp.hpp:172): out[monitor][sample], monitor = order of
+   the SJ_PROBE_MONITOR probes; cap = capacity in doubles */
+int sj_read_monitors(sj_sim* sim, int32_t inst, double* out, size_t cap);
+/* running DFT sums: out[dft_probe][freq][re, im] */
+int sj_read_dft(sj_sim* sim, int32_t inst, double* out, size_t cap);
+/* full component array converted to FP64 (dump_raw, src/disp.cpp:732-737) */
+int sj_read_field(sj_sim* sim, int32_t inst, int32_t component, double* out, size_t cap);
+/* overwrite one component (initial conditions / checkpoint restore) */
+int sj_write_field(sj_sim* sim, int32_t inst, int32_t component, const double* in, size_t n);
+/* per-component class map the stepper uses: out[3][nz][ny][nx] */
+int sj_read_class_map(sj_sim* sim, int32_t inst, uint8_t* out, size_t cap);
+/* largest |E| over the instance (divergence guard, src/disp.cpp:727-729) */
+int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out);
+
+/* ---------------------------------------------------------------- rasteriser */
+/* cgs_material_function::in_bound per E-component Yee point, on the device:
+   out_masks[3][nz][ny][nx] = bitmask of the scene regions containing the
+   point (composite_object::in, src/cgs.cpp:403-449). */
+int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out_masks);
+
+/* ---------------------------------------------------------------- host helpers */
+/* gaussian_src_time_phase::dipole (src/disp.cpp:378-400) / meep's
+   continuous_src_time, and the current the stepper injects at time t */
+int sj_source_dipole(const sj_source_desc* src, double t, double* re, double* im);
+int sj_source_current(const sj_source_desc* src, double t, double dt, double* re, double* im);
+/* gaussian_src_time_phase::last_time (src/disp.hpp:115) */
+double sj_source_last_time(const sj_source_desc* src);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SJ_H */

@@ -1,0 +1,1053 @@
+// Host side of the C ABI (include/sj.h): descriptor validation, the
+// structure builder (class maps -> material combos, meep-form ADE
+// coefficients, CPML profiles), source tables, probe stencils, device
+// allocation, stepping and read-back.
+//
+// Reference counterparts: structure_from_settings (src/disp.cpp:482-550),
+// the bound_geom constructor's source/monitor scan (src/disp.cpp:557-645),
+// bound_geom::run (src/disp.cpp:690-749).
+#include "sj_internal.h"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+using namespace sj;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct Fail {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& m) { throw Fail{code, m}; }
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) fail(SJ_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------------------ sources
+// gaussian_src_time_phase (src/disp.cpp:378-400): omega = 2 pi f,
+// phi = phase + pi, peak = (st + et)/2, cutoff = (et - st)/2 shrunk while the
+// envelope there is below 1e-100 and rounded to float, amp = 1/(-i omega).
+struct GaussParams {
+    double omega, width, phi, peak, cutoff;
+    std::complex<double> amp;
+};
+
+GaussParams gauss_params(const sj_source_desc& s) {
+    GaussParams g;
+    g.omega = 2 * M_PI * s.frequency;
+    g.width = s.width;
+    g.phi = s.phase + M_PI;
+    g.peak = 0.5 * (s.start_time + s.end_time);
+    g.cutoff = (s.end_time - s.start_time) * 0.5;
+    g.amp = 1.0 / std::complex<double>(0, -g.omega);
+    while (exp(-g.cutoff * g.cutoff / (2 * g.width * g.width)) < 1e-100) g.cutoff *= 0.9;
+    g.cutoff = float(g.cutoff);
+    return g;
+}
+
+std::complex<double> dipole(const sj_source_desc& s, double t) {
+    if (s.kind == SJ_SRC_GAUSSIAN) {
+        const GaussParams g = gauss_params(s);
+        const double tt = t - g.peak;
+        if (float(fabs(tt)) > g.cutoff) return 0.0;
+        return exp(-tt * tt / (2 * g.width * g.width)) * std::polar(1.0, -g.omega * tt - g.phi) * g.amp;
+    }
+    // continuous source: e^{-i w t}/(-i w) with tanh turn-on/turn-off ramps of
+    // width `width` and slowness 3 (meep's continuous_src_time)
+    const float rt = float(t);
+    if (rt < s.start_time || rt > s.end_time) return 0.0;
+    const std::complex<double> iw(0, -2 * M_PI * s.frequency);
+    if (s.width == 0.0) return std::exp(iw * t) / iw;
+    const double slowness = 3.0;
+    const double ts = (t - s.start_time) / s.width - slowness;
+    const double te = (s.end_time - t) / s.width - slowness;
+    return std::exp(iw * t) / iw * (1.0 + tanh(ts)) * (1.0 + tanh(te)) * 0.25;
+}
+
+std::complex<double> current(const sj_source_desc& s, double t, double dt) {
+    return (dipole(s, t) - dipole(s, t - dt)) / dt;
+}
+
+double last_time(const sj_source_desc& s) {
+    if (s.kind == SJ_SRC_GAUSSIAN) {
+        const GaussParams g = gauss_params(s);
+        return float(g.peak + g.cutoff);
+    }
+    return float(s.end_time);
+}
+
+// ------------------------------------------------------------------ helpers
+const double kOff[6][3] = {{0.5, 0, 0}, {0, 0.5, 0}, {0, 0, 0.5},
+                           {0, 0.5, 0.5}, {0.5, 0, 0.5}, {0.5, 0.5, 0}};
+
+// one instance as the host sees it
+template <typename real>
+struct HostInst {
+    sj_grid_desc grid{};
+    int nx = 0, ny = 0, nz = 0, px = 0;
+    double dx = 0, dt = 0;
+    int save_span = 1;
+    std::vector<sj_source_desc> srcs;
+    std::vector<double*> d_tab;      // per source
+    long long tab_cap = 0;
+    std::vector<int> probe_flags;
+    int n_mon = 0, n_dft = 0, n_freq = 0;
+    double* d_mon = nullptr;
+    long long mon_cap = 0;
+    std::vector<uint32_t> keys;      // combo -> (cx | cy<<8 | cz<<16)
+    long long voxels = 0;
+    double bytes_per_step = 0;
+    double last_source_time = 0;
+};
+
+}  // namespace
+
+struct sj_sim {
+    int precision = SJ_F64;
+    int schedule = SJ_SCHED_SPLIT;
+    int n_inst = 0;
+    std::vector<HostInst<double>> hi64;
+    std::vector<HostInst<float>> hi32;
+    std::vector<InstDev<double>> h64;
+    std::vector<InstDev<float>> h32;
+    void* d_table = nullptr;           // InstDev[n] + split prefix[n+1]
+    DevState* d_state = nullptr;
+    double* d_scratch = nullptr;       // small reductions
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long t = 0;                   // host mirror of the step counter
+    long long h2d = 0, d2h = 0;        // bytes copied across PCIe/C2C
+    int cur = 0;                       // host mirror of the ping-pong buffer
+    std::vector<void*> allocs;
+    std::string err;
+    // graph cache
+    cudaGraphExec_t graph = nullptr;
+    int graph_chunk = 0;
+    int graph_sched = -1;
+
+    ~sj_sim() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+    void* dalloc(size_t bytes, bool zero = true) {
+        void* p = nullptr;
+        if (bytes == 0) return nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) fail(SJ_E_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+        allocs.push_back(p);
+        if (zero) ck(cudaMemsetAsync(p, 0, bytes, stream), "cudaMemsetAsync");
+        return p;
+    }
+    void dfree(void* p) {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p);
+    }
+    template <typename T>
+    T* upload(const std::vector<T>& v) {
+        if (v.empty()) return nullptr;
+        T* p = (T*)dalloc(v.size() * sizeof(T), false);
+        ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+        h2d += (long long)(v.size() * sizeof(T));
+        return p;
+    }
+};
+
+namespace {
+
+// ------------------------------------------------------------------ validation
+void check_scene(const sj_scene_desc* sc) {
+    if (!sc) fail(SJ_E_INVALID, "material has neither class_map nor scene");
+    if (sc->n_regions < 0 || sc->n_regions > SJ_MAX_REGIONS)
+        fail(SJ_E_INVALID, "scene n_regions must be in [0, 8]");
+    int total = 0;
+    for (int r = 0; r < sc->n_regions; ++r) {
+        const sj_region_desc& g = sc->regions[r];
+        if (g.n_nodes < 1 || !g.nodes) fail(SJ_E_INVALID, "region without CSG nodes");
+        int depth = 0;
+        for (int q = 0; q < g.n_nodes; ++q) {
+            const int op = g.nodes[q].op;
+            if (op < 0) fail(SJ_E_INVALID, "negative CSG op");
+            if (op <= SJ_CSG_PLANE || op == SJ_CSG_CONST || op == SJ_CSG_NOOP)
+                ++depth;
+            else if (op == SJ_CSG_UNION || op == SJ_CSG_INTERSECT) {
+                if (depth < 2) fail(SJ_E_INVALID, "CSG program underflows its stack");
+                --depth;
+            } else if (op == SJ_CSG_PASS) {
+                if (depth < 1) fail(SJ_E_INVALID, "CSG program underflows its stack");
+            } else
+                fail(SJ_E_INVALID, "unknown CSG op " + std::to_string(op));
+            if (depth > 64) fail(SJ_E_INVALID, "CSG program deeper than 64");
+        }
+        if (depth != 1) fail(SJ_E_INVALID, "CSG program must leave exactly one value");
+        if (g.n_poles < 0 || (g.n_poles > 0 && (!g.poles || !g.sigma)))
+            fail(SJ_E_INVALID, "region poles/sigma missing");
+        total += g.n_nodes;
+    }
+    if (total > SJ_MAX_CSG_NODES * SJ_MAX_REGIONS) fail(SJ_E_INVALID, "too many CSG nodes");
+}
+
+void upload_scene(sj_sim* sim, const sj_scene_desc* sc, sj_csg_node** d_nodes, int** d_start) {
+    std::vector<sj_csg_node> nodes;
+    std::vector<int> start(1, 0);
+    for (int r = 0; r < sc->n_regions; ++r) {
+        const sj_region_desc& g = sc->regions[r];
+        nodes.insert(nodes.end(), g.nodes, g.nodes + g.n_nodes);
+        start.push_back((int)nodes.size());
+    }
+    if (nodes.empty()) nodes.push_back(sj_csg_node{});
+    *d_nodes = sim->upload(nodes);
+    *d_start = sim->upload(start);
+}
+
+// class table of a scene: class = bitmask of regions (src/disp.cpp:264-283)
+void scene_classes(const sj_scene_desc* sc, std::vector<double>& eps, std::vector<sj_pole>& poles,
+                   std::vector<double>& sigma, int& n_classes) {
+    const int R = sc->n_regions;
+    n_classes = 1 << R;
+    poles.clear();
+    std::vector<std::pair<int, double>> owner;  // (region, sigma)
+    for (int r = 0; r < R; ++r)
+        for (int q = 0; q < sc->regions[r].n_poles; ++q) {
+            poles.push_back(sc->regions[r].poles[q]);
+            owner.push_back({r, sc->regions[r].sigma[q]});
+        }
+    if ((int)poles.size() > SJ_MAX_POLES) fail(SJ_E_INVALID, "more than 8 susceptibilities in scene");
+    if (sc->combine != SJ_EPS_SUM && sc->combine != SJ_EPS_FIRST) fail(SJ_E_INVALID, "bad scene combine mode");
+    eps.assign(n_classes, 0.0);
+    sigma.assign((size_t)n_classes * poles.size(), 0.0);
+    const double def = sc->ambient_eps;
+    for (int m = 0; m < n_classes; ++m) {
+        int first = -1;  // first region containing the point (SJ_EPS_FIRST)
+        for (int r = 0; r < R && first < 0; ++r)
+            if ((m >> r) & 1) first = r;
+        if (sc->combine == SJ_EPS_FIRST) {
+            eps[m] = first >= 0 ? sc->regions[first].eps : def;
+        } else if (R == 0) {
+            eps[m] = def;
+        } else {
+            double ret = 0;
+            for (int r = 0; r < R; ++r) {
+                const double in = (m >> r) & 1;
+                ret += def + (sc->regions[r].eps - def) * in / 1.0;
+            }
+            eps[m] = ret;
+        }
+        for (size_t p = 0; p < poles.size(); ++p) {
+            double in = (m >> owner[p].first) & 1;
+            if (sc->combine == SJ_EPS_FIRST && owner[p].first != first) in = 0;
+            sigma[(size_t)m * poles.size() + p] = 0.0 + (owner[p].second - 0.0) * in / 1.0;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ builder
+template <typename real>
+void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, InstDev<real>& I) {
+    cudaStream_t st = sim->stream;
+    memset(&I, 0, sizeof(I));
+    const sj_grid_desc& g = d.grid;
+    if (g.nx < 1 || g.ny < 1 || g.nz < 1) fail(SJ_E_INVALID, "grid dimensions must be >= 1");
+    if (!(g.dx > 0)) fail(SJ_E_INVALID, "grid dx must be > 0");
+    if ((long long)g.nx * g.ny * g.nz > (1ll << 40)) fail(SJ_E_INVALID, "grid too large");
+    H.grid = g;
+    H.nx = g.nx, H.ny = g.ny, H.nz = g.nz;
+    H.px = (g.nx + PITCH_ALIGN - 1) / PITCH_ALIGN * PITCH_ALIGN;
+    H.dx = g.dx;
+    H.dt = g.dt > 0 ? g.dt : 0.5 * g.dx;
+    H.save_span = d.save_span > 0 ? d.save_span : 1;
+    const int nx = H.nx, ny = H.ny, nz = H.nz, px = H.px;
+    const long long plane = (long long)px * ny, vol = plane * nz;
+    I.nx = nx, I.ny = ny, I.nz = nz, I.px = px;
+    I.plane = plane, I.vol = vol;
+    I.S = (real)(H.dt / H.dx);
+    I.dt = H.dt;
+    I.save_span = H.save_span;
+    H.voxels = (long long)nx * ny * nz;
+
+    // ---- fields, both ping-pong buffers
+    for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 6; ++c) I.F[b][c] = (real*)sim->dalloc(vol * sizeof(real));
+
+    // ---- material classes per E-component point (pitched [3][nz][ny][px])
+    const sj_material_desc& m = d.material;
+    std::vector<double> eps;
+    std::vector<sj_pole> poles;
+    std::vector<double> sigma;
+    int n_classes = 0;
+    const long long cpitch = vol;
+    uint8_t* d_cls = (uint8_t*)sim->dalloc(3 * cpitch, false);
+    if (m.class_map) {
+        if (m.n_classes < 1 || m.n_classes > 255) fail(SJ_E_INVALID, "n_classes must be in [1, 255]");
+        if (!m.eps_inf) fail(SJ_E_INVALID, "eps_inf missing");
+        if (m.n_poles < 0 || m.n_poles > SJ_MAX_POLES) fail(SJ_E_INVALID, "n_poles must be in [0, 8]");
+        if (m.n_poles > 0 && (!m.poles || !m.sigma)) fail(SJ_E_INVALID, "poles/sigma missing");
+        n_classes = m.n_classes;
+        eps.assign(m.eps_inf, m.eps_inf + n_classes);
+        poles.assign(m.poles, m.poles + m.n_poles);
+        sigma.assign(m.sigma, m.sigma + (size_t)n_classes * m.n_poles);
+        for (int c = 0; c < 3; ++c)
+            ck(cudaMemcpy2D(d_cls + c * cpitch, px, m.class_map + (size_t)c * nx * ny * nz, nx, nx,
+                            (size_t)ny * nz, cudaMemcpyHostToDevice),
+               "class map upload");
+        sim->h2d += 3ll * nx * ny * nz;
+    } else {
+        check_scene(m.scene);
+        scene_classes(m.scene, eps, poles, sigma, n_classes);
+        sj_csg_node* d_nodes;
+        int* d_start;
+        upload_scene(sim, m.scene, &d_nodes, &d_start);
+        ck(launch_rasterize(d_nodes, d_start, m.scene->n_regions, nx, ny, nz, H.dx, g.origin, d_cls,
+                            cpitch, px, st),
+           "rasterize");
+    }
+    for (int c = 0; c < n_classes; ++c)
+        if (!(eps[c] != 0.0) || !std::isfinite(eps[c])) fail(SJ_E_INVALID, "eps_inf must be finite and nonzero");
+
+    // ---- combos: distinct (class_x, class_y, class_z) triples
+    {
+        uint32_t* d_bitmap = (uint32_t*)sim->dalloc((1u << 24) / 8);
+        ck(launch_combo_mark(d_cls, cpitch, nx, ny, nz, px, d_bitmap, st), "combo mark");
+        std::vector<uint32_t> bitmap((1u << 24) / 32);
+        ck(cudaMemcpyAsync(bitmap.data(), d_bitmap, bitmap.size() * 4, cudaMemcpyDeviceToHost, st), "bitmap");
+        sim->d2h += (long long)bitmap.size() * 4;
+        ck(cudaStreamSynchronize(st), "combo sync");
+        H.keys.clear();
+        for (uint32_t w = 0; w < bitmap.size(); ++w) {
+            uint32_t bits = bitmap[w];
+            while (bits) {
+                const int b = __builtin_ctz(bits);
+                bits &= bits - 1;
+                H.keys.push_back(w * 32 + b);
+            }
+        }
+        sim->dfree(d_bitmap);
+        if (H.keys.size() > 256) fail(SJ_E_INVALID, "more than 256 distinct material combos");
+        for (uint32_t k : H.keys)
+            for (int c = 0; c < 3; ++c)
+                if ((int)((k >> (8 * c)) & 255) >= n_classes)
+                    fail(SJ_E_INVALID, "class map holds a class index >= n_classes");
+        uint32_t* d_keys = sim->upload(H.keys);
+        uint8_t* d_combo = (uint8_t*)sim->dalloc(vol);
+        ck(launch_combo_assign(d_cls, cpitch, nx, ny, nz, px, d_keys, (int)H.keys.size(), d_combo, st),
+           "combo assign");
+        ck(cudaStreamSynchronize(st), "combo sync");
+        sim->dfree(d_keys);
+        sim->dfree(d_cls);
+        I.combo = d_combo;
+    }
+
+    // ---- meep-form ADE coefficients (lorentzian_susceptibility::update_P)
+    const int np = (int)poles.size();
+    I.n_poles = np;
+    std::vector<double> Cp(np);
+    for (int p = 0; p < np; ++p) {
+        const double w = 2 * M_PI * poles[p].omega_0, gm = 2 * M_PI * poles[p].gamma;
+        const double dt = H.dt;
+        const double den = 1 + gm * dt / 2;
+        const double L = poles[p].drude ? 0.0 : 1.0;
+        I.A[p] = (real)((2 - w * w * dt * dt * L) / den);
+        I.B[p] = (real)(-(1 - gm * dt / 2) / den);
+        Cp[p] = w * w * dt * dt / den;
+    }
+    const int nk = (int)H.keys.size();
+    I.n_combos = nk;
+    I.ncoef = 3 + 3 * np;
+    std::vector<real> coef((size_t)nk * I.ncoef);
+    std::vector<uint8_t> cflag(nk, 0);
+    for (int q = 0; q < nk; ++q) {
+        for (int c = 0; c < 3; ++c) {
+            const int cl = (H.keys[q] >> (8 * c)) & 255;
+            coef[(size_t)q * I.ncoef + c] = (real)(1.0 / eps[cl]);
+            for (int p = 0; p < np; ++p) {
+                const double cs = Cp[p] * sigma[(size_t)cl * np + p];
+                coef[(size_t)q * I.ncoef + 3 + 3 * p + c] = (real)cs;
+                if (cs != 0.0) cflag[q] |= 1;
+            }
+        }
+    }
+    I.coef = sim->upload(coef);
+    I.cflag = sim->upload(cflag);
+
+    // ---- dispersive bounding box and polarisation storage
+    {
+        std::vector<unsigned long long> hist(256);
+        unsigned long long* d_hist = (unsigned long long*)sim->dalloc(256 * 8);
+        ck(launch_combo_hist(I.combo, nx, ny, nz, px, d_hist, st), "combo hist");
+        ck(cudaMemcpyAsync(hist.data(), d_hist, 256 * 8, cudaMemcpyDeviceToHost, st), "hist");
+        int box[6] = {INT_MAX, INT_MAX, INT_MAX, -1, -1, -1};
+        bool any = false;
+        for (int q = 0; q < nk; ++q) any |= (cflag[q] & 1) != 0;
+        int* d_box = nullptr;
+        if (any) {
+            d_box = (int*)sim->dalloc(sizeof(box), false);
+            ck(cudaMemcpyAsync(d_box, box, sizeof(box), cudaMemcpyHostToDevice, st), "box");
+            ck(launch_disp_bbox(I.combo, I.cflag, nx, ny, nz, px, d_box, st), "bbox");
+            ck(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, st), "box");
+        }
+        ck(cudaStreamSynchronize(st), "bbox sync");
+        sim->dfree(d_hist);
+        sim->dfree(d_box);
+        long long n_disp_pole = 0;  // sum over poles of voxels carrying the pole
+        for (int q = 0; q < nk; ++q)
+            for (int p = 0; p < np; ++p) {
+                bool on = false;
+                for (int c = 0; c < 3; ++c) on |= coef[(size_t)q * I.ncoef + 3 + 3 * p + c] != 0;
+                if (on) n_disp_pole += (long long)hist[q];
+            }
+        if (any && box[3] >= 0) {
+            for (int a = 0; a < 3; ++a) {
+                I.dlo[a] = box[a];
+                I.dn[a] = box[3 + a] - box[a] + 1;
+            }
+            I.dvol = (long long)I.dn[0] * I.dn[1] * I.dn[2];
+            I.P = (real*)sim->dalloc((size_t)np * 6 * I.dvol * sizeof(real));
+        }
+        H.bytes_per_step = (double)H.voxels * (12.0 * sizeof(real) + 1) + (double)n_disp_pole * 12.0 * sizeof(real);
+    }
+
+    // ---- CPML profiles and slabs
+    const sj_pml_desc& pm = d.pml;
+    const double R = pm.r_asymptotic > 0 ? pm.r_asymptotic : 1e-15;
+    const double pw = pm.power > 0 ? pm.power : 2.0;
+    for (int a = 0; a < 3; ++a) {
+        const int n = a == 0 ? nx : (a == 1 ? ny : nz);
+        const double o = g.origin[a], L = n * H.dx;
+        const double dlo = pm.thickness[a][0], dhi = pm.thickness[a][1];
+        if (dlo < 0 || dhi < 0) fail(SJ_E_INVALID, "PML thickness must be >= 0");
+        auto sigma_at = [&](double q) {
+            double s = 0;
+            if (dlo > 0 && q < o + dlo) {
+                const double u = (o + dlo - q) / dlo;
+                s += -(pw + 1) * log(R) / (2 * dlo) * pow(u, pw);
+            }
+            if (dhi > 0 && q > o + L - dhi) {
+                const double u = (q - (o + L - dhi)) / dhi;
+                s += -(pw + 1) * log(R) / (2 * dhi) * pow(u, pw);
+            }
+            return s;
+        };
+        std::vector<real> prof(4 * (size_t)n);
+        std::vector<char> on(n, 0);
+        for (int i = 0; i < n; ++i) {
+            for (int h = 0; h < 2; ++h) {
+                const double q = o + (i + 0.5 * h) * H.dx;
+                const double s = sigma_at(q);
+                const double b = exp(-(s + pm.alpha) * H.dt);
+                const double c = s > 0 ? s / (s + pm.alpha) * (b - 1) : 0.0;
+                prof[(2 * h) * n + i] = (real)b;
+                prof[(2 * h + 1) * n + i] = (real)c;
+                if (s > 0) on[i] = 1;
+            }
+        }
+        int pl = 0, ph = 0;
+        while (pl < n && on[pl]) ++pl;
+        while (ph < n - pl && on[n - 1 - ph]) ++ph;
+        for (int i = pl; i < n - ph; ++i)
+            if (on[i]) fail(SJ_E_INVALID, "PML profile is not confined to the faces");
+        I.pl[a] = pl, I.ph[a] = ph;
+        I.prof[a] = sim->upload(prof);
+        const long long w = pl + ph;
+        I.slabvol[a] = a == 0 ? (long long)nz * ny * w : (a == 1 ? (long long)nz * w * px : w * (long long)ny * px);
+        if (w > 0) {
+            I.psiE[a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
+            I.psiH[0][a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
+            I.psiH[1][a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
+        }
+        const long long slab_vox = a == 0 ? (long long)nz * ny * w : (a == 1 ? (long long)nz * w * nx : w * (long long)ny * nx);
+        H.bytes_per_step += (double)slab_vox * 4 * 2 * sizeof(real);
+    }
+
+    // ---- sources: separable weights on the component's own grid
+    if (d.n_sources < 0 || d.n_sources > SJ_MAX_SOURCES) fail(SJ_E_INVALID, "n_sources must be in [0, 4]");
+    I.n_src = d.n_sources;
+    H.srcs.assign(d.sources, d.sources + d.n_sources);
+    H.last_source_time = 0;
+    for (int s = 0; s < d.n_sources; ++s) {
+        const sj_source_desc& sd = d.sources[s];
+        if (sd.component < 0 || sd.component > 5) fail(SJ_E_INVALID, "source component out of range");
+        if (sd.kind != SJ_SRC_GAUSSIAN && sd.kind != SJ_SRC_CONTINUOUS) fail(SJ_E_INVALID, "bad source kind");
+        if (sd.kind == SJ_SRC_GAUSSIAN && !(sd.width > 0)) fail(SJ_E_INVALID, "Gaussian width must be > 0");
+        if (!(sd.frequency > 0)) fail(SJ_E_INVALID, "source frequency must be > 0");
+        SrcDev<real>& sv = I.src[s];
+        sv.comp = sd.component;
+        for (int a = 0; a < 3; ++a) {
+            const int n = a == 0 ? nx : (a == 1 ? ny : nz);
+            const double lo = std::min(sd.lo[a], sd.hi[a]), hi = std::max(sd.lo[a], sd.hi[a]);
+            const double off = kOff[sd.component][a];
+            std::vector<double> w(n, 0.0);
+            if (hi - lo <= 1e-9 * H.dx) {
+                // zero extent: linear interpolation onto the two nearest points, / dx
+                const double u = (lo - g.origin[a]) / H.dx - off;
+                const double i0 = floor(u);
+                const double f = u - i0;
+                const long long a0 = (long long)i0;
+                if (a0 >= 0 && a0 < n) w[a0] += (1 - f) / H.dx;
+                if (a0 + 1 >= 0 && a0 + 1 < n) w[a0 + 1] += f / H.dx;
+            } else {
+                // finite extent: overlap of each point's dual cell with [lo, hi], / dx
+                for (int i = 0; i < n; ++i) {
+                    const double q = g.origin[a] + (i + off) * H.dx;
+                    const double ov = std::min(hi, q + 0.5 * H.dx) - std::max(lo, q - 0.5 * H.dx);
+                    if (ov > 0) w[i] = ov / H.dx;
+                }
+            }
+            int first = -1, last = -1;
+            for (int i = 0; i < n; ++i)
+                if (w[i] != 0.0) {
+                    if (first < 0) first = i;
+                    last = i;
+                }
+            if (first < 0) {  // outside the grid: empty stencil
+                first = 0;
+                last = -1;
+            }
+            sv.lo[a] = first;
+            sv.n[a] = last - first + 1;
+            std::vector<real> wr(std::max(1, sv.n[a]));
+            for (int i = 0; i < sv.n[a]; ++i) wr[i] = (real)w[first + i];
+            sv.w[a] = sim->upload(wr);
+        }
+        H.last_source_time = std::max(H.last_source_time, last_time(sd));
+    }
+    H.d_tab.assign(d.n_sources, nullptr);
+    H.tab_cap = 0;
+
+    // ---- probes: trilinear stencils on the component's grid
+    if (d.n_probes < 0) fail(SJ_E_INVALID, "n_probes < 0");
+    if (d.n_freqs < 0 || d.n_freqs > 256) fail(SJ_E_INVALID, "n_freqs must be in [0, 256]");
+    I.n_probe = d.n_probes;
+    std::vector<int> pcomp(d.n_probes), pmon(d.n_probes, -1), pdft(d.n_probes, -1);
+    std::vector<long long> pidx(8 * (size_t)d.n_probes, -1);
+    std::vector<double> pw8(8 * (size_t)d.n_probes, 0.0);
+    for (int p = 0; p < d.n_probes; ++p) {
+        const sj_probe_desc& pd = d.probes[p];
+        if (pd.component < 0 || pd.component > 5) fail(SJ_E_INVALID, "probe component out of range");
+        pcomp[p] = pd.component;
+        if (pd.flags & SJ_PROBE_MONITOR) pmon[p] = H.n_mon++;
+        if (pd.flags & SJ_PROBE_DFT) pdft[p] = H.n_dft++;
+        long long i0[3];
+        double f[3];
+        for (int a = 0; a < 3; ++a) {
+            const double u = (pd.pos[a] - g.origin[a]) / H.dx - kOff[pd.component][a];
+            const double fl = floor(u);
+            i0[a] = (long long)fl;
+            f[a] = u - fl;
+        }
+        for (int m8 = 0; m8 < 8; ++m8) {
+            const int di = m8 & 1, dj = (m8 >> 1) & 1, dk = (m8 >> 2) & 1;
+            const long long ii = i0[0] + di, jj = i0[1] + dj, kk = i0[2] + dk;
+            const double w = (di ? f[0] : 1 - f[0]) * (dj ? f[1] : 1 - f[1]) * (dk ? f[2] : 1 - f[2]);
+            if (ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz) {
+                pidx[8 * (size_t)p + m8] = kk * plane + jj * px + ii;
+                pw8[8 * (size_t)p + m8] = w;
+            }
+        }
+    }
+    I.n_mon = H.n_mon, I.n_dft = H.n_dft, I.n_freq = d.n_freqs;
+    H.n_freq = d.n_freqs;
+    I.probe_comp = sim->upload(pcomp);
+    I.probe_idx = sim->upload(pidx);
+    I.probe_w = sim->upload(pw8);
+    I.probe_mon = sim->upload(pmon);
+    I.probe_dft = sim->upload(pdft);
+    if (d.n_freqs > 0) I.freqs = sim->upload(std::vector<double>(d.freqs, d.freqs + d.n_freqs));
+    if (H.n_dft > 0 && d.n_freqs > 0)
+        I.dft = (double2*)sim->dalloc((size_t)H.n_dft * d.n_freqs * sizeof(double2));
+    I.mon = nullptr;
+    I.mon_cap = 0;
+}
+
+// ------------------------------------------------------------------ stepping support
+template <typename real>
+std::vector<HostInst<real>>& hostv(sj_sim* s);
+template <>
+std::vector<HostInst<double>>& hostv<double>(sj_sim* s) { return s->hi64; }
+template <>
+std::vector<HostInst<float>>& hostv<float>(sj_sim* s) { return s->hi32; }
+template <typename real>
+std::vector<InstDev<real>>& devv(sj_sim* s);
+template <>
+std::vector<InstDev<double>>& devv<double>(sj_sim* s) { return s->h64; }
+template <>
+std::vector<InstDev<float>>& devv<float>(sj_sim* s) { return s->h32; }
+
+long long split_blocks(const InstDev<double>& I) { return split_block_count_f64(I); }
+long long split_blocks(const InstDev<float>& I) { return split_block_count_f32(I); }
+
+template <typename real>
+void upload_table(sj_sim* sim) {
+    auto& dv = devv<real>(sim);
+    const int n = sim->n_inst;
+    std::vector<char> buf(n * sizeof(InstDev<real>) + (n + 1) * sizeof(long long));
+    memcpy(buf.data(), dv.data(), n * sizeof(InstDev<real>));
+    long long* pre = reinterpret_cast<long long*>(buf.data() + n * sizeof(InstDev<real>));
+    pre[0] = 0;
+    for (int q = 0; q < n; ++q) pre[q + 1] = pre[q] + split_blocks(dv[q]);
+    if (!sim->d_table) sim->d_table = sim->dalloc(buf.size(), false);
+    ck(cudaStreamSynchronize(sim->stream), "sync before table upload");
+    ck(cudaMemcpy(sim->d_table, buf.data(), buf.size(), cudaMemcpyHostToDevice), "table upload");
+    sim->h2d += (long long)buf.size();
+}
+
+// Make sure source tables and monitor buffers cover steps [0, t_end).
+template <typename real>
+void ensure_capacity(sj_sim* sim, long long t_end) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    bool changed = false;
+    for (int q = 0; q < sim->n_inst; ++q) {
+        HostInst<real>& H = hv[q];
+        InstDev<real>& I = dv[q];
+        if (!H.srcs.empty() && H.tab_cap < t_end) {
+            const long long cap = std::max(t_end, 2 * H.tab_cap);
+            ck(cudaStreamSynchronize(sim->stream), "sync");
+            for (size_t s = 0; s < H.srcs.size(); ++s) {
+                std::vector<double> tab(cap);
+                const sj_source_desc& sd = H.srcs[s];
+                const double half = sd.component < 3 ? 0.5 : 0.0;
+                for (long long nn = 0; nn < cap; ++nn) {
+                    const double tt = ((double)nn + half) * H.dt;
+                    const std::complex<double> a(sd.amplitude[0], sd.amplitude[1]);
+                    tab[nn] = H.dt * std::real(a * current(sd, tt, H.dt));
+                }
+                sim->dfree(H.d_tab[s]);
+                H.d_tab[s] = sim->upload(tab);
+                I.src[s].tab = H.d_tab[s];
+            }
+            H.tab_cap = cap;
+            changed = true;
+        }
+        if (H.n_mon > 0) {
+            const long long need = (t_end + H.save_span - 1) / H.save_span;
+            if (H.mon_cap < need) {
+                const long long cap = std::max(need, 2 * H.mon_cap);
+                double* nb = (double*)sim->dalloc((size_t)cap * H.n_mon * sizeof(double));
+                ck(cudaStreamSynchronize(sim->stream), "sync");
+                if (H.d_mon)
+                    ck(cudaMemcpy(nb, H.d_mon, (size_t)H.mon_cap * H.n_mon * sizeof(double),
+                                  cudaMemcpyDeviceToDevice),
+                       "mon grow");
+                sim->dfree(H.d_mon);
+                H.d_mon = nb;
+                H.mon_cap = cap;
+                I.mon = nb;
+                I.mon_cap = cap;
+                changed = true;
+            }
+        }
+    }
+    if (changed) upload_table<real>(sim);
+}
+
+template <typename real>
+cudaError_t launch_one(sj_sim* sim) {
+    auto& dv = devv<real>(sim);
+    const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
+    if (sim->schedule == SJ_SCHED_FUSED)
+        return launch_fused_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream, 0);
+    return launch_split_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream);
+}
+
+template <typename real>
+void do_steps(sj_sim* sim, long long n) {
+    ensure_capacity<real>(sim, sim->t + n);
+    for (long long q = 0; q < n; ++q) ck(launch_one<real>(sim), "step launch");
+    sim->t += n;
+    if (sim->schedule == SJ_SCHED_FUSED && (n & 1)) sim->cur ^= 1;
+}
+
+template <typename real>
+void do_steps_graph(sj_sim* sim, long long n, int chunk) {
+    if (chunk < 1) fail(SJ_E_INVALID, "chunk must be >= 1");
+    ensure_capacity<real>(sim, sim->t + n);
+    if (!sim->graph || sim->graph_chunk != chunk || sim->graph_sched != sim->schedule) {
+        if (sim->graph) cudaGraphExecDestroy(sim->graph);
+        sim->graph = nullptr;
+        cudaStream_t cs;
+        ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+        cudaStream_t saved = sim->stream;
+        sim->stream = cs;
+        cudaGraph_t gr;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int q = 0; q < chunk && e == cudaSuccess; ++q) e = launch_one<real>(sim);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &gr);
+            if (e == cudaSuccess) e = e2;
+        }
+        sim->stream = saved;
+        cudaStreamDestroy(cs);
+        ck(e, "graph capture");
+        e = cudaGraphInstantiate(&sim->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        ck(e, "graph instantiate");
+        sim->graph_chunk = chunk;
+        sim->graph_sched = sim->schedule;
+    }
+    long long left = n;
+    while (left >= chunk) {
+        ck(cudaGraphLaunch(sim->graph, sim->stream), "graph launch");
+        left -= chunk;
+    }
+    for (long long q = 0; q < left; ++q) ck(launch_one<real>(sim), "step launch");
+    sim->t += n;
+    if (sim->schedule == SJ_SCHED_FUSED && (n & 1)) sim->cur ^= 1;
+}
+
+int finish(sj_sim* sim, int code, const std::string& msg) {
+    if (sim)
+        sim->err = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+#define SJ_TRY(sim) try {
+#define SJ_CATCH(sim)                                              \
+    }                                                              \
+    catch (const Fail& f) {                                        \
+        return finish(sim, f.code, f.msg);                         \
+    }                                                              \
+    catch (const std::exception& ex) {                             \
+        return finish(sim, SJ_E_INVALID, ex.what());               \
+    }                                                              \
+    return SJ_OK;
+
+int check_status(sj_sim* sim) {
+    DevState st;
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    ck(cudaMemcpy(&st, sim->d_state, sizeof(st), cudaMemcpyDeviceToHost), "state");
+    if (st.status != 0) fail(st.status, "a kernel reported status " + std::to_string(st.status));
+    if (st.step != sim->t) fail(SJ_E_CUDA, "device step counter disagrees with host");
+    return 0;
+}
+
+template <typename real>
+void read_field_t(sj_sim* sim, int inst, int comp, double* out) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    const HostInst<real>& H = hv[inst];
+    const InstDev<real>& I = dv[inst];
+    std::vector<real> tmp((size_t)H.nx * H.ny * H.nz);
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    ck(cudaMemcpy2D(tmp.data(), H.nx * sizeof(real), I.F[sim->cur][comp], H.px * sizeof(real),
+                    H.nx * sizeof(real), (size_t)H.ny * H.nz, cudaMemcpyDeviceToHost),
+       "field read");
+    for (size_t q = 0; q < tmp.size(); ++q) out[q] = (double)tmp[q];
+}
+
+template <typename real>
+void write_field_t(sj_sim* sim, int inst, int comp, const double* in) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    const HostInst<real>& H = hv[inst];
+    const InstDev<real>& I = dv[inst];
+    std::vector<real> tmp((size_t)H.nx * H.ny * H.nz);
+    for (size_t q = 0; q < tmp.size(); ++q) tmp[q] = (real)in[q];
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    ck(cudaMemcpy2D(I.F[sim->cur][comp], H.px * sizeof(real), tmp.data(), H.nx * sizeof(real),
+                    H.nx * sizeof(real), (size_t)H.ny * H.nz, cudaMemcpyHostToDevice),
+       "field write");
+}
+
+template <typename real>
+void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    hv.resize(n);
+    dv.resize(n);
+    for (int q = 0; q < n; ++q) build_instance<real>(sim, insts[q], hv[q], dv[q]);
+    upload_table<real>(sim);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int sj_abi_version(void) { return SJ_ABI_VERSION; }
+
+int64_t sj_abi_struct_size(int32_t which) {
+    switch (which) {
+        case 0: return sizeof(sj_grid_desc);
+        case 1: return sizeof(sj_pole);
+        case 2: return sizeof(sj_csg_node);
+        case 3: return sizeof(sj_region_desc);
+        case 4: return sizeof(sj_scene_desc);
+        case 5: return sizeof(sj_material_desc);
+        case 6: return sizeof(sj_pml_desc);
+        case 7: return sizeof(sj_source_desc);
+        case 8: return sizeof(sj_probe_desc);
+        case 9: return sizeof(sj_instance_desc);
+        default: return -1;
+    }
+}
+
+const char* sj_last_error(const sj_sim* sim) {
+    return sim ? sim->err.c_str() : g_create_error.c_str();
+}
+
+int sj_batch_create(int32_t n, const sj_instance_desc* insts, int32_t precision, sj_sim** out) {
+    if (!out) return finish(nullptr, SJ_E_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n < 1 || !insts) return finish(nullptr, SJ_E_INVALID, "need at least one instance");
+    if (precision != SJ_F64 && precision != SJ_F32) return finish(nullptr, SJ_E_INVALID, "bad precision");
+    std::unique_ptr<sj_sim> sim(new sj_sim());
+    try {
+        sim->precision = precision;
+        sim->n_inst = n;
+        ck(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "stream create");
+        sim->own_stream = true;
+        sim->d_state = (DevState*)sim->dalloc(sizeof(DevState));
+        sim->d_scratch = (double*)sim->dalloc(64);
+        if (precision == SJ_F64)
+            create_t<double>(sim.get(), n, insts);
+        else
+            create_t<float>(sim.get(), n, insts);
+        ck(cudaStreamSynchronize(sim->stream), "create sync");
+    } catch (const Fail& f) {
+        return finish(nullptr, f.code, f.msg);
+    } catch (const std::exception& ex) {
+        return finish(nullptr, SJ_E_NOMEM, ex.what());
+    }
+    *out = sim.release();
+    return SJ_OK;
+}
+
+int sj_create(const sj_instance_desc* inst, int32_t precision, sj_sim** out) {
+    return sj_batch_create(1, inst, precision, out);
+}
+
+int sj_destroy(sj_sim* sim) {
+    delete sim;
+    return SJ_OK;
+}
+
+int sj_set_stream(sj_sim* sim, void* stream) {
+    if (!sim) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    if (sim->own_stream) cudaStreamDestroy(sim->stream);
+    if (stream) {
+        sim->stream = (cudaStream_t)stream;
+        sim->own_stream = false;
+    } else {
+        ck(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "stream create");
+        sim->own_stream = true;
+    }
+    SJ_CATCH(sim)
+}
+
+int sj_set_schedule(sj_sim* sim, int32_t schedule) {
+    if (!sim) return SJ_E_INVALID;
+    if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT)
+        return finish(sim, SJ_E_INVALID, "unknown schedule");
+    sim->schedule = schedule;
+    return SJ_OK;
+}
+
+int sj_synchronize(sj_sim* sim) {
+    if (!sim) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    check_status(sim);
+    SJ_CATCH(sim)
+}
+
+int sj_step(sj_sim* sim, int64_t n) {
+    if (!sim) return SJ_E_INVALID;
+    if (n < 0) return finish(sim, SJ_E_INVALID, "n_steps < 0");
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        do_steps<double>(sim, n);
+    else
+        do_steps<float>(sim, n);
+    SJ_CATCH(sim)
+}
+
+int sj_step_graph(sj_sim* sim, int64_t n, int32_t chunk) {
+    if (!sim) return SJ_E_INVALID;
+    if (n < 0) return finish(sim, SJ_E_INVALID, "n_steps < 0");
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        do_steps_graph<double>(sim, n, chunk);
+    else
+        do_steps_graph<float>(sim, n, chunk);
+    SJ_CATCH(sim)
+}
+
+int64_t sj_steps_done(const sj_sim* sim) { return sim ? sim->t : -1; }
+
+int sj_transfer_bytes(const sj_sim* sim, int64_t* h2d, int64_t* d2h) {
+    if (!sim || !h2d || !d2h) return SJ_E_INVALID;
+    *h2d = sim->h2d;
+    *d2h = sim->d2h;
+    return SJ_OK;
+}
+int32_t sj_n_instances(const sj_sim* sim) { return sim ? sim->n_inst : -1; }
+
+#define INST_GET(field, bad)                                                                  \
+    if (!sim || inst < 0 || inst >= sim->n_inst) return bad;                                  \
+    return sim->precision == SJ_F64 ? sim->hi64[inst].field : sim->hi32[inst].field;
+
+double sj_dt(const sj_sim* sim, int32_t inst) { INST_GET(dt, NAN) }
+double sj_time(const sj_sim* sim, int32_t inst) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return NAN;
+    return sim->t * sj_dt(sim, inst);
+}
+double sj_last_source_time(const sj_sim* sim, int32_t inst) { INST_GET(last_source_time, NAN) }
+int64_t sj_voxels(const sj_sim* sim, int32_t inst) { INST_GET(voxels, -1) }
+double sj_bytes_per_step(const sj_sim* sim, int32_t inst) { INST_GET(bytes_per_step, NAN) }
+int64_t sj_n_samples(const sj_sim* sim, int32_t inst) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return -1;
+    const int ss = sim->precision == SJ_F64 ? sim->hi64[inst].save_span : sim->hi32[inst].save_span;
+    return (sim->t + ss - 1) / ss;
+}
+
+int sj_read_monitors(sj_sim* sim, int32_t inst, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    check_status(sim);
+    const int nm = sim->precision == SJ_F64 ? sim->hi64[inst].n_mon : sim->hi32[inst].n_mon;
+    double* dm = sim->precision == SJ_F64 ? sim->hi64[inst].d_mon : sim->hi32[inst].d_mon;
+    const long long ns = sj_n_samples(sim, inst);
+    if ((size_t)nm * ns > cap) fail(SJ_E_RANGE, "output buffer too small for monitors");
+    if (nm == 0 || ns == 0) return SJ_OK;
+    std::vector<double> tmp((size_t)nm * ns);
+    ck(cudaMemcpy(tmp.data(), dm, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost), "mon read");
+    sim->d2h += (long long)(tmp.size() * sizeof(double));
+    for (long long s = 0; s < ns; ++s)
+        for (int m = 0; m < nm; ++m) out[(size_t)m * ns + s] = tmp[(size_t)s * nm + m];
+    SJ_CATCH(sim)
+}
+
+int sj_read_dft(sj_sim* sim, int32_t inst, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    check_status(sim);
+    int nd, nf;
+    double2* p;
+    if (sim->precision == SJ_F64) {
+        nd = sim->hi64[inst].n_dft, nf = sim->hi64[inst].n_freq, p = sim->h64[inst].dft;
+    } else {
+        nd = sim->hi32[inst].n_dft, nf = sim->hi32[inst].n_freq, p = sim->h32[inst].dft;
+    }
+    if ((size_t)nd * nf * 2 > cap) fail(SJ_E_RANGE, "output buffer too small for DFT");
+    if (nd && nf) ck(cudaMemcpy(out, p, (size_t)nd * nf * sizeof(double2), cudaMemcpyDeviceToHost), "dft read");
+    sim->d2h += (long long)nd * nf * sizeof(double2);
+    SJ_CATCH(sim)
+}
+
+int sj_read_field(sj_sim* sim, int32_t inst, int32_t comp, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || comp < 0 || comp > 5) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if ((size_t)sj_voxels(sim, inst) > cap) fail(SJ_E_RANGE, "output buffer too small for field");
+    if (sim->precision == SJ_F64)
+        read_field_t<double>(sim, inst, comp, out);
+    else
+        read_field_t<float>(sim, inst, comp, out);
+    SJ_CATCH(sim)
+}
+
+int sj_write_field(sj_sim* sim, int32_t inst, int32_t comp, const double* in, size_t n) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || comp < 0 || comp > 5) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if ((size_t)sj_voxels(sim, inst) != n) fail(SJ_E_RANGE, "field size mismatch");
+    if (sim->precision == SJ_F64)
+        write_field_t<double>(sim, inst, comp, in);
+    else
+        write_field_t<float>(sim, inst, comp, in);
+    SJ_CATCH(sim)
+}
+
+int sj_read_class_map(sj_sim* sim, int32_t inst, uint8_t* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    const bool d64 = sim->precision == SJ_F64;
+    const int nx = d64 ? sim->hi64[inst].nx : sim->hi32[inst].nx;
+    const int ny = d64 ? sim->hi64[inst].ny : sim->hi32[inst].ny;
+    const int nz = d64 ? sim->hi64[inst].nz : sim->hi32[inst].nz;
+    const int px = d64 ? sim->hi64[inst].px : sim->hi32[inst].px;
+    const std::vector<uint32_t>& keys = d64 ? sim->hi64[inst].keys : sim->hi32[inst].keys;
+    const uint8_t* combo = d64 ? sim->h64[inst].combo : sim->h32[inst].combo;
+    const size_t nv = (size_t)nx * ny * nz;
+    if (3 * nv > cap) fail(SJ_E_RANGE, "output buffer too small for class map");
+    std::vector<uint8_t> tmp(nv);
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    ck(cudaMemcpy2D(tmp.data(), nx, combo, px, nx, (size_t)ny * nz, cudaMemcpyDeviceToHost), "combo read");
+    for (size_t q = 0; q < nv; ++q)
+        for (int c = 0; c < 3; ++c) out[c * nv + q] = (uint8_t)((keys[tmp[q]] >> (8 * c)) & 255);
+    SJ_CATCH(sim)
+}
+
+int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || !out) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        ck(launch_max_abs_e<double>(sim->h64[inst], sim->cur, sim->d_scratch, sim->stream), "max");
+    else
+        ck(launch_max_abs_e<float>(sim->h32[inst], sim->cur, sim->d_scratch, sim->stream), "max");
+    ck(cudaMemcpyAsync(out, sim->d_scratch, sizeof(double), cudaMemcpyDeviceToHost, sim->stream), "max read");
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    SJ_CATCH(sim)
+}
+
+int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out) {
+    if (!grid || !scene || !out) return finish(nullptr, SJ_E_INVALID, "NULL argument");
+    try {
+        if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0))
+            fail(SJ_E_INVALID, "bad grid");
+        check_scene(scene);
+        sj_sim tmp;
+        ck(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking), "stream");
+        tmp.own_stream = true;
+        sj_csg_node* d_nodes;
+        int* d_start;
+        upload_scene(&tmp, scene, &d_nodes, &d_start);
+        const int nx = grid->nx, ny = grid->ny, nz = grid->nz;
+        const long long nv = (long long)nx * ny * nz;
+        uint8_t* d = (uint8_t*)tmp.dalloc(3 * nv);
+        ck(launch_rasterize(d_nodes, d_start, scene->n_regions, nx, ny, nz, grid->dx, grid->origin, d, nv,
+                            nx, tmp.stream),
+           "rasterize");
+        ck(cudaMemcpyAsync(out, d, 3 * nv, cudaMemcpyDeviceToHost, tmp.stream), "mask read");
+        ck(cudaStreamSynchronize(tmp.stream), "sync");
+    } catch (const Fail& f) {
+        return finish(nullptr, f.code, f.msg);
+    }
+    return SJ_OK;
+}
+
+int sj_source_dipole(const sj_source_desc* src, double t, double* re, double* im) {
+    if (!src || !re || !im) return SJ_E_INVALID;
+    const std::complex<double> v = dipole(*src, t);
+    *re = v.real();
+    *im = v.imag();
+    return SJ_OK;
+}
+
+int sj_source_current(const sj_source_desc* src, double t, double dt, double* re, double* im) {
+    if (!src || !re || !im || !(dt > 0)) return SJ_E_INVALID;
+    const std::complex<double> v = current(*src, t, dt);
+    *re = v.real();
+    *im = v.imag();
+    return SJ_OK;
+}
+
+double sj_source_last_time(const sj_source_desc* src) { return src ? last_time(*src) : NAN; }
+
+}  // extern "C"

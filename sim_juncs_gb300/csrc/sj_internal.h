@@ -1,0 +1,112 @@
+// Internal structures shared by the host driver (sj_host.cu) and the
+// kernels (sj_step.cu, sj_raster.cu).  Nothing here crosses the C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/sj.h"
+
+namespace sj {
+
+constexpr int MAXP = SJ_MAX_POLES;
+constexpr int MAXS = SJ_MAX_SOURCES;
+
+// Row pitch of every per-voxel array, in elements.  Rows start on 128-byte
+// boundaries for FP32 and 256-byte boundaries for FP64.
+constexpr int PITCH_ALIGN = 32;
+
+// One separable source stencil: J(i,j,k,n) = tab[n] * w0[i-lo0] * w1[j-lo1] * w2[k-lo2],
+// with tab[n] = dt * Re[amp * current(t_n)] precomputed on the host in FP64.
+template <typename real>
+struct SrcDev {
+    int comp;            // SJ_EX..SJ_HZ
+    int lo[3], n[3];     // index box on the component's own Yee grid
+    const real* w[3];    // per-axis weights
+    const double* tab;   // [steps]
+};
+
+// Device-side view of one simulation instance.
+template <typename real>
+struct InstDev {
+    int nx, ny, nz, px;         // px = row pitch (elements), >= nx
+    long long plane, vol;       // px*ny, px*ny*nz
+    real S;                     // Courant number dt/dx
+    double dt;
+    real* F[2][6];              // [ping-pong][Ex..Hz]
+
+    // materials: one byte per voxel selects a "combo" = (class at Ex, Ey, Ez)
+    const uint8_t* combo;       // [nz][ny][px]
+    const real* coef;           // [n_combos][ncoef]: inv_eps[3], then Csig[p][3]
+    const uint8_t* cflag;       // [n_combos]: bit 0 = some pole has sigma != 0
+    int n_combos, ncoef;
+    int n_poles;
+    real A[MAXP], B[MAXP];
+
+    // polarisation storage, dense over the bounding box of dispersive voxels
+    int dlo[3], dn[3];
+    long long dvol;
+    real* P;                    // [n_poles][2 levels: n, n-1][3 comps][dvol]
+
+    // CPML: slab thickness (cells) per axis and face, profiles, psi storage
+    int pl[3], ph[3];
+    const real* prof[3];        // per axis: b_int[n], c_int[n], b_half[n], c_half[n]
+    long long slabvol[3];
+    real* psiE[3];              // per axis: [2 comps][slabvol]
+    real* psiH[2][3];           // [ping-pong][axis]: [2 comps][slabvol]
+
+    int n_src;
+    SrcDev<real> src[MAXS];
+
+    // probes (monitors and DFT points)
+    int n_probe, n_mon, n_dft, n_freq, save_span;
+    const int* probe_comp;      // [n_probe]
+    const long long* probe_idx; // [n_probe][8] element offsets, -1 = outside
+    const double* probe_w;      // [n_probe][8]
+    const int* probe_mon;       // [n_probe] monitor column or -1
+    const int* probe_dft;       // [n_probe] DFT row or -1
+    const double* freqs;        // [n_freq]
+    double* mon;                // [mon_cap][n_mon]
+    long long mon_cap;
+    double2* dft;               // [n_dft][n_freq]
+};
+
+// Step counter and status kept in device memory so that graph replays need
+// no per-launch arguments.
+struct DevState {
+    long long step;     // absolute step index n of the next step
+    unsigned int done;  // blocks finished in the current launch
+    int cur;            // ping-pong buffer holding E^n, H^{n-1/2}
+    int status;         // sticky error code set by kernels (0 = fine)
+    int _pad;
+};
+
+// Launch helpers implemented in sj_step.cu.
+template <typename real>
+cudaError_t launch_probe(const InstDev<real>* d_insts, const InstDev<real>* h_insts, int n_inst,
+                         DevState* st, cudaStream_t s);
+long long split_block_count_f64(const InstDev<double>& I);
+long long split_block_count_f32(const InstDev<float>& I);
+template <typename real>
+cudaError_t launch_split_step(const InstDev<real>* d_insts, const InstDev<real>* h_insts,
+                              int n_inst, DevState* st, cudaStream_t s);
+template <typename real>
+cudaError_t launch_fused_step(const InstDev<real>* d_insts, const InstDev<real>* h_insts,
+                              int n_inst, DevState* st, cudaStream_t s, int tile_y);
+template <typename real>
+cudaError_t launch_max_abs_e(const InstDev<real>& h_inst, int buf, double* d_out, cudaStream_t s);
+
+// Launch helpers implemented in sj_raster.cu.
+cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_start,
+                             int n_regions, int nx, int ny, int nz, double dx,
+                             const double* origin, uint8_t* d_masks, long long mask_pitch_elems,
+                             int px, cudaStream_t s);
+cudaError_t launch_combo_mark(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
+                              int px, uint32_t* d_bitmap, cudaStream_t s);
+cudaError_t launch_combo_assign(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
+                                int px, const uint32_t* d_keys, int n_keys, uint8_t* d_combo,
+                                cudaStream_t s);
+cudaError_t launch_combo_hist(const uint8_t* d_combo, int nx, int ny, int nz, int px,
+                              unsigned long long* d_hist, cudaStream_t s);
+cudaError_t launch_disp_bbox(const uint8_t* d_combo, const uint8_t* d_cflag, int nx, int ny,
+                             int nz, int px, int* d_box, cudaStream_t s);
+
+}  // namespace sj

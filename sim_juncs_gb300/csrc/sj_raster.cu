@@ -1,0 +1,232 @@
+// Device rasteriser (material classes per E-component Yee point) and the
+// combo/bounding-box passes that turn class maps into the stepper's
+// one-byte-per-voxel material index.
+//
+// The CSG evaluation restates composite_object::in and the primitives'
+// in() (src/cgs.cpp:34-120, 403-449) with the reference's operation order:
+// matrix rows are summed left to right starting from 0 (src/geometry.hpp:88-99),
+// dot products left to right (src/geometry.hpp:199-201), and no fused
+// multiply-add, so that points lying exactly on a face get the same answer.
+#include "sj_internal.h"
+
+namespace sj {
+
+__device__ __forceinline__ void mat_vec(const double* __restrict__ m, double x, double y, double z,
+                                        double& ox, double& oy, double& oz) {
+    ox = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(m[0], x)), __dmul_rn(m[1], y)), __dmul_rn(m[2], z));
+    oy = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(m[3], x)), __dmul_rn(m[4], y)), __dmul_rn(m[5], z));
+    oz = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(m[6], x)), __dmul_rn(m[7], y)), __dmul_rn(m[8], z));
+}
+
+// Evaluate one region's postfix program at r; returns in_root(r) in {0,1}.
+// The operand stack is a 64-bit word: push = shift left, pop = shift right.
+__device__ int eval_program(const sj_csg_node* __restrict__ nodes, int n, double x, double y,
+                            double z) {
+    unsigned long long stk = 0;
+    for (int q = 0; q < n; ++q) {
+        const sj_csg_node& nd = nodes[q];
+        const int op = nd.op;
+        int v = 0;
+        if (op <= SJ_CSG_PLANE) {
+            double rx, ry, rz;
+            mat_vec(nd.m, x, y, z, rx, ry, rz);
+            if (op == SJ_CSG_PLANE) {
+                const double d = __dadd_rn(__dadd_rn(__dmul_rn(rx, nd.p[0]), __dmul_rn(ry, nd.p[1])),
+                                           __dmul_rn(rz, nd.p[2]));
+                v = d > nd.p[3] ? 0 : 1;
+            } else {
+                double qx, qy, qz;
+                mat_vec(nd.t, __dsub_rn(rx, nd.c[0]), __dsub_rn(ry, nd.c[1]), __dsub_rn(rz, nd.c[2]),
+                        qx, qy, qz);
+                bool out;
+                if (op == SJ_CSG_BOX) {
+                    out = fabs(qx) > nd.p[0] || fabs(qy) > nd.p[1] || fabs(qz) > nd.p[2];
+                } else if (op == SJ_CSG_SPHERE) {
+                    const double s2 = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(qx, qx)), __dmul_rn(qy, qy)),
+                                                __dmul_rn(qz, qz));
+                    out = __dsqrt_rn(s2) > nd.p[0];
+                } else {  // cylinder: p = height, r1^2, r2^2
+                    const double h = nd.p[0], r1 = nd.p[1], r2 = nd.p[2];
+                    if (qz < 0 || qz > h) {
+                        out = true;
+                    } else {
+                        const double cr = __dadd_rn(__dmul_rn(qx, qx), __dmul_rn(qy, qy));
+                        out = __dmul_rn(cr, h) > __dadd_rn(__dmul_rn(__dsub_rn(r2, r1), qz), __dmul_rn(r1, h));
+                    }
+                }
+                v = out ? nd.invert : 1 - nd.invert;
+            }
+            stk = (stk << 1) | (unsigned long long)v;
+        } else if (op == SJ_CSG_UNION || op == SJ_CSG_INTERSECT) {
+            const int b = (int)(stk & 1ull);
+            stk >>= 1;
+            const int a = (int)(stk & 1ull);
+            stk >>= 1;
+            v = nd.invert ^ (op == SJ_CSG_UNION ? (a | b) : (a & b));
+            stk = (stk << 1) | (unsigned long long)v;
+        } else if (op == SJ_CSG_PASS) {
+            const int a = (int)(stk & 1ull);
+            stk = (stk & ~1ull) | (unsigned long long)(nd.invert ^ a);
+        } else if (op == SJ_CSG_CONST) {
+            stk = (stk << 1) | (unsigned long long)(nd.invert & 1);
+        } else {  // NOOP
+            stk = (stk << 1);
+        }
+    }
+    return (int)(stk & 1ull);
+}
+
+// One thread per voxel: masks for the Ex, Ey and Ez points.
+__global__ void k_rasterize(const sj_csg_node* __restrict__ nodes, const int* __restrict__ rstart,
+                            int n_regions, int nx, int ny, int nz, double dx, double ox, double oy,
+                            double oz, uint8_t* __restrict__ masks, long long cpitch, int px) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    for (int c = 0; c < 3; ++c) {
+        const double x = __dadd_rn(ox, __dmul_rn((double)i + (c == 0 ? 0.5 : 0.0), dx));
+        const double y = __dadd_rn(oy, __dmul_rn((double)j + (c == 1 ? 0.5 : 0.0), dx));
+        const double z = __dadd_rn(oz, __dmul_rn((double)k + (c == 2 ? 0.5 : 0.0), dx));
+        unsigned m = 0;
+        for (int g = 0; g < n_regions; ++g) {
+            const int s = rstart[g], e = rstart[g + 1];
+            if (eval_program(nodes + s, e - s, x, y, z)) m |= 1u << g;
+        }
+        masks[c * cpitch + o] = (uint8_t)m;
+    }
+}
+
+cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_start, int n_regions,
+                             int nx, int ny, int nz, double dx, const double* origin,
+                             uint8_t* d_masks, long long mask_pitch_elems, int px, cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    k_rasterize<<<blocks, 256, 0, s>>>(d_nodes, d_region_start, n_regions, nx, ny, nz, dx,
+                                       origin[0], origin[1], origin[2], d_masks, mask_pitch_elems, px);
+    return cudaGetLastError();
+}
+
+// Mark every (class_x, class_y, class_z) triple present in a 2^24-bit set.
+__global__ void k_combo_mark(const uint8_t* __restrict__ cls, long long cpitch, int nx, int ny,
+                             int nz, int px, uint32_t* __restrict__ bitmap) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    const uint32_t key = (uint32_t)cls[o] | ((uint32_t)cls[cpitch + o] << 8) |
+                         ((uint32_t)cls[2 * cpitch + o] << 16);
+    const uint32_t bit = 1u << (key & 31u);
+    uint32_t* w = bitmap + (key >> 5);
+    if ((*((volatile uint32_t*)w) & bit) == 0) atomicOr(w, bit);
+}
+
+cudaError_t launch_combo_mark(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
+                              int px, uint32_t* d_bitmap, cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    k_combo_mark<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(d_cls, cpitch, nx, ny, nz, px, d_bitmap);
+    return cudaGetLastError();
+}
+
+// Replace each voxel's triple by its index in the sorted key list.
+__global__ void k_combo_assign(const uint8_t* __restrict__ cls, long long cpitch, int nx, int ny,
+                               int nz, int px, const uint32_t* __restrict__ keys, int n_keys,
+                               uint8_t* __restrict__ combo) {
+    __shared__ uint32_t sk[256];
+    for (int q = threadIdx.x; q < n_keys; q += blockDim.x) sk[q] = keys[q];
+    __syncthreads();
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    const uint32_t key = (uint32_t)cls[o] | ((uint32_t)cls[cpitch + o] << 8) |
+                         ((uint32_t)cls[2 * cpitch + o] << 16);
+    int lo = 0, hi = n_keys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sk[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    combo[o] = (uint8_t)lo;
+}
+
+cudaError_t launch_combo_assign(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
+                                int px, const uint32_t* d_keys, int n_keys, uint8_t* d_combo,
+                                cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    k_combo_assign<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(d_cls, cpitch, nx, ny, nz, px,
+                                                                   d_keys, n_keys, d_combo);
+    return cudaGetLastError();
+}
+
+// Bounding box of voxels whose combo carries a polarisation: box = {min i,j,k, max i,j,k}.
+__global__ void k_disp_bbox(const uint8_t* __restrict__ combo, const uint8_t* __restrict__ cflag,
+                            int nx, int ny, int nz, int px, int* box) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    if (cflag[combo[o]] & 1) {
+        atomicMin(box + 0, i);
+        atomicMin(box + 1, j);
+        atomicMin(box + 2, k);
+        atomicMax(box + 3, i);
+        atomicMax(box + 4, j);
+        atomicMax(box + 5, k);
+    }
+}
+
+cudaError_t launch_disp_bbox(const uint8_t* d_combo, const uint8_t* d_cflag, int nx, int ny,
+                             int nz, int px, int* d_box, cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    k_disp_bbox<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(d_combo, d_cflag, nx, ny, nz, px, d_box);
+    return cudaGetLastError();
+}
+
+}  // namespace sj
+
+namespace sj {
+// 256-bin histogram of the combo map (voxel counts per material combo).
+__global__ void k_combo_hist(const uint8_t* __restrict__ combo, int nx, int ny, int nz, int px,
+                             unsigned long long* __restrict__ hist) {
+    __shared__ unsigned int h[256];
+    for (int q = threadIdx.x; q < 256; q += blockDim.x) h[q] = 0;
+    __syncthreads();
+    const long long total = (long long)nx * ny * nz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % nx);
+        const long long r = t / nx;
+        const int j = (int)(r % ny);
+        const int k = (int)(r / ny);
+        atomicAdd(&h[combo[((long long)k * ny + j) * px + i]], 1u);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < 256; q += blockDim.x)
+        if (h[q]) atomicAdd(hist + q, (unsigned long long)h[q]);
+}
+
+cudaError_t launch_combo_hist(const uint8_t* d_combo, int nx, int ny, int nz, int px,
+                              unsigned long long* d_hist, cudaStream_t s) {
+    k_combo_hist<<<608, 256, 0, s>>>(d_combo, nx, ny, nz, px, d_hist);
+    return cudaGetLastError();
+}
+}  // namespace sj

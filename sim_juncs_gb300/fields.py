@@ -1,0 +1,174 @@
+"""``Fields``: the Python handle on the C ABI, standing where the reference
+holds its ``meep::fields`` member (src/disp.hpp:175-177).
+
+Method names follow the calls the reference makes on that object
+(src/disp.cpp:557-749): ``step``, ``time``, ``dt``, ``last_source_time``,
+``get_field`` (monitor read-back) and ``output`` of a raw component.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .spec import Instance
+
+_PREC = {"f64": _abi.F64, "f32": _abi.F32, _abi.F64: _abi.F64, _abi.F32: _abi.F32}
+_SCHED = {"fused": _abi.SCHED_FUSED, "split": _abi.SCHED_SPLIT,
+          _abi.SCHED_FUSED: _abi.SCHED_FUSED, _abi.SCHED_SPLIT: _abi.SCHED_SPLIT}
+
+
+class Fields:
+    """One or many simulation instances stepped by the CUDA library."""
+
+    def __init__(self, instances, precision="f64", schedule="fused", stream=None):
+        self.lib = _abi.load_library()
+        if isinstance(instances, Instance):
+            instances = [instances]
+        self.instances = list(instances)
+        n = len(self.instances)
+        descs = (_abi.InstanceDesc * n)()
+        self._holders = []
+        for q, inst in enumerate(self.instances):
+            d, h = inst.to_c()
+            descs[q] = d
+            self._holders.append(h)
+        self.precision = _PREC[precision]
+        handle = C.c_void_p()
+        _abi.check(self.lib, self.lib.sj_batch_create(n, descs, self.precision, C.byref(handle)))
+        self.handle = handle
+        self._holders = None  # the library copied everything it needs
+        self.set_schedule(schedule)
+        if stream is not None:
+            self.set_stream(stream)
+
+    # ------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sj_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, code):
+        return _abi.check(self.lib, code, self.handle)
+
+    def set_stream(self, stream):
+        """Run on `stream` (a cudaStream_t as int, or a torch.cuda.Stream)."""
+        ptr = getattr(stream, "cuda_stream", stream)
+        self._ck(self.lib.sj_set_stream(self.handle, C.c_void_p(ptr)))
+
+    def set_schedule(self, schedule):
+        self._ck(self.lib.sj_set_schedule(self.handle, _SCHED[schedule]))
+
+    def synchronize(self):
+        self._ck(self.lib.sj_synchronize(self.handle))
+
+    # ------------------------------------------------------------ stepping
+    def step(self, n=1):
+        """n iterations of the reference loop body (asynchronous)."""
+        self._ck(self.lib.sj_step(self.handle, int(n)))
+
+    def step_graph(self, n, chunk=50):
+        self._ck(self.lib.sj_step_graph(self.handle, int(n), int(chunk)))
+
+    # ------------------------------------------------------------ queries
+    @property
+    def n_instances(self):
+        return len(self.instances)
+
+    @property
+    def steps_done(self):
+        return self.lib.sj_steps_done(self.handle)
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes this sim has copied so far."""
+        a, b = C.c_int64(), C.c_int64()
+        self._ck(self.lib.sj_transfer_bytes(self.handle, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def dt(self, inst=0):
+        return self.lib.sj_dt(self.handle, inst)
+
+    def time(self, inst=0):
+        return self.lib.sj_time(self.handle, inst)
+
+    def last_source_time(self, inst=0):
+        return self.lib.sj_last_source_time(self.handle, inst)
+
+    def voxels(self, inst=None):
+        if inst is None:
+            return sum(self.lib.sj_voxels(self.handle, q) for q in range(self.n_instances))
+        return self.lib.sj_voxels(self.handle, inst)
+
+    def bytes_per_step(self, inst=None):
+        if inst is None:
+            return sum(self.lib.sj_bytes_per_step(self.handle, q) for q in range(self.n_instances))
+        return self.lib.sj_bytes_per_step(self.handle, inst)
+
+    def n_samples(self, inst=0):
+        return self.lib.sj_n_samples(self.handle, inst)
+
+    # ------------------------------------------------------------ read-back
+    def monitors(self, inst=0):
+        """field_times: [monitor][sample] (float64)."""
+        nm = self.instances[inst].n_monitors
+        ns = self.n_samples(inst)
+        out = np.zeros((nm, ns), dtype=np.float64)
+        self._ck(self.lib.sj_read_monitors(self.handle, inst,
+                                           out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
+
+    def dft(self, inst=0):
+        """Running DFT sums: complex [dft_probe][freq]."""
+        nd = self.instances[inst].n_dft
+        nf = len(self.instances[inst].freqs)
+        out = np.zeros((nd, nf, 2), dtype=np.float64)
+        self._ck(self.lib.sj_read_dft(self.handle, inst,
+                                      out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def get_array(self, component, inst=0):
+        """Full component array [nz][ny][nx] as float64 (dump_raw)."""
+        g = self.instances[inst].grid
+        out = np.zeros((g.nz, g.ny, g.nx), dtype=np.float64)
+        self._ck(self.lib.sj_read_field(self.handle, inst, component,
+                                        out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
+
+    def set_array(self, component, values, inst=0):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._ck(self.lib.sj_write_field(self.handle, inst, component,
+                                         v.ctypes.data_as(C.POINTER(C.c_double)), v.size))
+
+    def class_map(self, inst=0):
+        g = self.instances[inst].grid
+        out = np.zeros((3, g.nz, g.ny, g.nx), dtype=np.uint8)
+        self._ck(self.lib.sj_read_class_map(self.handle, inst,
+                                            out.ctypes.data_as(C.POINTER(C.c_uint8)), out.size))
+        return out
+
+    def max_abs_e(self, inst=0):
+        v = C.c_double()
+        self._ck(self.lib.sj_max_abs_e(self.handle, inst, C.byref(v)))
+        return v.value
+
+
+def rasterize(grid, scene):
+    """Region bitmasks at the Ex/Ey/Ez points of `grid` ([3][nz][ny][nx] uint8)."""
+    from .spec import scene_to_c
+    lib = _abi.load_library()
+    sc, h = scene_to_c(scene)
+    out = np.zeros((3, grid.nz, grid.ny, grid.nx), dtype=np.uint8)
+    g = grid.to_c()
+    _abi.check(lib, lib.sj_rasterize(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return out

@@ -1,0 +1,151 @@
+"""Parity of the CUDA stepper with the FP64 CPU oracle, through the C ABI.
+
+Bar: FP64 fields, monitors and DFT sums within 1e-10 of the oracle,
+relative to the largest magnitude of the compared quantity; FP32 gap
+monitors within 1e-4 of FP64 (the target for the FP32 path).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleFields, rasterize as oracle_rasterize
+from sim_juncs_gb300 import _abi
+from sim_juncs_gb300.configs import bowtie_instance, junction_instance, sweep_instances
+from sim_juncs_gb300.fields import Fields, rasterize
+from sim_juncs_gb300.spec import Grid
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-4
+
+
+def rel(a, b):
+    scale = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a)))
+
+
+def compare_fields(f, o, tol, inst=0):
+    for c in range(6):
+        g = f.get_array(c, inst)
+        r = o.get_array(c)
+        assert rel(g, r) <= tol, (c, rel(g, r))
+
+
+@pytest.mark.parametrize("schedule", ["split", "fused"])
+def test_junction_f64_matches_oracle(lib, oracle_lib, schedule):
+    inst = junction_instance()            # 64^3, 20 px/um, 2000 steps
+    f = Fields(inst, "f64", schedule)
+    o = OracleFields(inst)
+    for upto in (1, 10, 400, 2000):
+        n = upto - o.steps_done
+        f.step(n)
+        o.step(n)
+        compare_fields(f, o, TOL64)
+    assert f.steps_done == 2000
+    mg, mo = f.monitors(), o.monitors()
+    assert mg.shape == mo.shape == (8, 100)
+    assert rel(mg, mo) <= TOL64
+    dg, do = f.dft(), o.dft()
+    assert rel(dg, do) <= TOL64
+    assert np.max(np.abs(mo[:4])) > 0.1           # the gap is lit
+
+
+def test_junction_class_map_matches_oracle(lib, oracle_lib):
+    inst = junction_instance()
+    f = Fields(inst, "f64", "split")
+    o = OracleFields(inst)
+    np.testing.assert_array_equal(f.class_map(), o.class_map())
+
+
+@pytest.mark.parametrize("n,res", [(64, 20.0), (48, 15.0)])
+def test_rasterizer_matches_oracle_junction(lib, oracle_lib, n, res):
+    inst = junction_instance(n=n, res=res)
+    g = Grid(n, n, n, 1.0 / res)
+    np.testing.assert_array_equal(rasterize(g, inst.material), oracle_rasterize(g, inst.material))
+
+
+def test_rasterizer_matches_oracle_bowtie(lib, oracle_lib):
+    inst = bowtie_instance(nx=128, ny=128, nz=96, res=10.0)
+    g = inst.grid
+    dev = rasterize(g, inst.material)
+    ref = oracle_rasterize(g, inst.material)
+    np.testing.assert_array_equal(dev, ref)
+    assert (dev & 1).any() and (dev & 2).any()
+
+
+@pytest.mark.parametrize("schedule", ["split", "fused"])
+def test_f32_gap_field_within_1e4_of_f64(lib, schedule):
+    inst = junction_instance()
+    f64 = Fields(inst, "f64", schedule)
+    f32 = Fields(inst, "f32", schedule)
+    f64.step(2000)
+    f32.step(2000)
+    m64, m32 = f64.monitors(), f32.monitors()
+    assert rel(m32[:4], m64[:4]) <= TOL32, rel(m32[:4], m64[:4])
+    assert rel(f32.dft()[:4], f64.dft()[:4]) <= TOL32
+
+
+@pytest.mark.parametrize("schedule", ["split", "fused"])
+def test_batch_of_uneven_grids_matches_oracle(lib, oracle_lib, schedule):
+    insts = [junction_instance(n=n, res=r, phase=ph, amplitude=a, probe_components=("Ex", "Ez"))
+             for (n, r, ph, a) in ((32, 10.0, 0.3, 2.0), (45, 14.0, 1.7, 0.5), (40, 12.5, 4.0, 1.0))]
+    f = Fields(insts, "f64", schedule)
+    f.step(300)
+    for q, inst in enumerate(insts):
+        o = OracleFields(inst)
+        o.step(300)
+        assert rel(f.monitors(q), o.monitors()) <= TOL64
+        assert rel(f.dft(q), o.dft()) <= TOL64
+        compare_fields(f, o, TOL64, q)
+
+
+@pytest.mark.parametrize("schedule", ["split", "fused"])
+def test_graph_replay_matches_plain_launches(lib, schedule):
+    inst = junction_instance(n=40, res=12.5)
+    a = Fields(inst, "f32", schedule)
+    b = Fields(inst, "f32", schedule)
+    a.step(173)
+    b.step_graph(173, chunk=25)
+    assert a.steps_done == b.steps_done == 173
+    for c in range(6):
+        np.testing.assert_array_equal(a.get_array(c), b.get_array(c))
+    np.testing.assert_array_equal(a.monitors(), b.monitors())
+
+
+def test_fused_and_split_agree_bitwise_f64(lib):
+    inst = junction_instance(n=48, res=15.0)
+    a = Fields(inst, "f64", "split")
+    b = Fields(inst, "f64", "fused")
+    a.step(137)
+    b.step(137)
+    for c in range(6):
+        assert rel(b.get_array(c), a.get_array(c)) <= 1e-13
+
+
+def test_write_read_roundtrip_and_queries(lib):
+    inst = junction_instance(n=32, res=10.0)
+    f = Fields(inst, "f64")
+    x = np.random.default_rng(3).standard_normal((32, 32, 32))
+    f.set_array(_abi.HY, x)
+    np.testing.assert_array_equal(f.get_array(_abi.HY), x)
+    assert f.dt() == pytest.approx(inst.grid.dt)
+    f.step(7)
+    assert f.time() == pytest.approx(7 * inst.grid.dt)
+    assert f.n_samples() == 1
+    assert f.last_source_time() == pytest.approx(20.0)
+    assert f.max_abs_e() >= 0
+
+
+def test_invalid_descriptors_are_rejected(lib):
+    inst = junction_instance(n=32, res=10.0)
+    inst.sources[0].component = 9
+    with pytest.raises(_abi.SJError) as e:
+        Fields(inst, "f64")
+    assert e.value.code == _abi.SJ_E_INVALID
+
+
+def test_sweep_instances_build(lib):
+    insts = sweep_instances(per_size=1)
+    f = Fields(insts, "f32")
+    f.step(5)
+    assert f.voxels() == 96 ** 3 + 128 ** 3 + 192 ** 3
