@@ -160,6 +160,9 @@ def run_ours(args):
 
     insts, cfg = workload_instances(args.workload, rank)
     f = Fields(insts, "f32", args.schedule, stream=torch.cuda.current_stream())
+    if args.schedule == "fused":
+        ty, zs, ring, _ = f.autotune(steps=2)
+        cfg = dict(cfg, tile=f"32x{ty}", zseg=zs, tma_ring=ring, tiling="autotuned")
     has_probes = any(i.probes for i in insts)
     lps = (1 if args.schedule == "fused" else 2) + (1 if has_probes and args.schedule == "split" else 0)
     voxels = f.voxels()
@@ -210,6 +213,8 @@ def fp64_leg(torch, args):
     from sim_juncs_gb300.fields import Fields
     inst = configs.bowtie_instance()
     f = Fields(inst, "f64", args.schedule, stream=torch.cuda.current_stream())
+    if args.schedule == "fused":
+        f.autotune(steps=2)
     steps = max(5, args.steps // 4)
     secs, _ = time_steps(f, torch, steps, 3, 1)
     peak, kind = measured_peak()

@@ -254,6 +254,16 @@ int sj_set_stream(sj_sim* sim, void* cuda_stream);
 int sj_set_schedule(sj_sim* sim, int32_t schedule);
 int sj_synchronize(sj_sim* sim);
 
+/* fused-schedule tiling: tile_y in {4, 8, 16} rows per block, z segments of
+   zseg planes (each block marches one segment), TMA ring of `ring` planes
+   (3 or 5) */
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t zseg, int32_t ring);
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* zseg, int32_t* ring);
+/* time every tiling candidate with `steps` launches that leave the state
+   untouched, keep the fastest and report it (any output may be NULL) */
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* zseg, int32_t* ring,
+                float* ms_per_step);
+
 /* ---------------------------------------------------------------- stepping */
 /* n_steps iterations of the loop body at src/disp.cpp:719-741: sample
    monitors when step % save_span == 0, accumulate DFTs, then fields.step().

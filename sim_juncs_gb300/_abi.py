@@ -104,6 +104,10 @@ SIGNATURES = {
     "sj_set_stream": (C.c_int, [_P, _P]),
     "sj_set_schedule": (C.c_int, [_P, C.c_int32]),
     "sj_synchronize": (C.c_int, [_P]),
+    "sj_set_tiling": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "sj_get_tiling": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "sj_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                              C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
     "sj_step": (C.c_int, [_P, C.c_int64]),
     "sj_step_graph": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "sj_steps_done": (C.c_int64, [_P]),

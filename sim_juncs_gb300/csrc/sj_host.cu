@@ -8,6 +8,9 @@
 // bound_geom::run (src/disp.cpp:690-749).
 #include "sj_internal.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -136,6 +139,12 @@ struct sj_sim {
     cudaGraphExec_t graph = nullptr;
     int graph_chunk = 0;
     int graph_sched = -1;
+    // fused schedule: tiling, tensor maps, block prefixes
+    int f_ty = 8, f_zs = 64, f_ns = 5;
+    bool fused_ready = false;
+    FusedLaunch fl{};
+    void* d_fpre = nullptr;
+    void* d_tmaps = nullptr;
 
     ~sj_sim() {
         if (stream) cudaStreamSynchronize(stream);
@@ -655,13 +664,139 @@ void ensure_capacity(sj_sim* sim, long long t_end) {
     if (changed) upload_table<real>(sim);
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        ck(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+           "cuTensorMapEncodeTiled lookup");
+        if (q != cudaDriverEntryPointSuccess || !p) fail(SJ_E_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// Tensor maps, tiling and block prefixes of the fused schedule.
+template <typename real>
+void prepare_fused(sj_sim* sim) {
+    if (sim->fused_ready) return;
+    auto& dv = devv<real>(sim);
+    const int n = sim->n_inst, ty = sim->f_ty;
+    auto encode = tensor_map_encoder();
+    std::vector<CUtensorMap> maps((size_t)n * 13);
+    std::vector<long long> pre(2 * (n + 1), 0);
+    const int thr = fused_block_threads(ty);
+    for (int q = 0; q < n; ++q) {
+        InstDev<real>& I = dv[q];
+        const cuuint64_t dims[3] = {(cuuint64_t)I.nx, (cuuint64_t)I.ny, (cuuint64_t)I.nz};
+        const cuuint32_t es[3] = {1, 1, 1};
+        auto enc = [&](CUtensorMap* m, CUtensorMapDataType dt, void* base, size_t esize, cuuint32_t bx,
+                       cuuint32_t by) {
+            const cuuint64_t strides[2] = {(cuuint64_t)I.px * esize, (cuuint64_t)I.plane * esize};
+            const cuuint32_t box[3] = {bx, by, 1};
+            CUresult r = encode(m, dt, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) fail(SJ_E_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        };
+        const CUtensorMapDataType fdt =
+            sizeof(real) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        const cuuint32_t bx = (cuuint32_t)fused_box_width<real>();
+        CUtensorMap* m = &maps[(size_t)q * 13];
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 3; ++c) {
+                enc(m + b * 3 + c, fdt, I.F[b][c], sizeof(real), bx, (cuuint32_t)(ty + 2));      // E
+                enc(m + 6 + b * 3 + c, fdt, I.F[b][3 + c], sizeof(real), bx, (cuuint32_t)(ty + 1));  // H
+            }
+        enc(m + 12, CU_TENSOR_MAP_DATA_TYPE_UINT8, const_cast<uint8_t*>(I.combo), 1, 32, (cuuint32_t)ty);
+        I.f_ntx = (I.nx + 31) / 32;
+        I.f_nty = (I.ny + ty - 1) / ty;
+        I.f_zs = std::max(1, std::min(sim->f_zs, I.nz));
+        I.f_nzs = (I.nz + I.f_zs - 1) / I.f_zs;
+        pre[q + 1] = pre[q] + (long long)I.f_ntx * I.f_nty * I.f_nzs;
+        pre[n + 1 + q + 1] = pre[n + 1 + q] + (I.n_probe + thr - 1) / thr;
+    }
+    sim->dfree(sim->d_tmaps);
+    sim->dfree(sim->d_fpre);
+    sim->d_tmaps = sim->upload(maps);
+    sim->d_fpre = sim->upload(pre);
+    for (int q = 0; q < n; ++q) dv[q].tmap = reinterpret_cast<const CUtensorMap*>(sim->d_tmaps) + (size_t)q * 13;
+    FusedLaunch& fl = sim->fl;
+    fl.ty = ty;
+    fl.nslot = sim->f_ns;
+    fl.n_items = pre[n];
+    fl.n_probe_blocks = pre[2 * n + 1];
+    fl.d_item_pre = reinterpret_cast<const long long*>(sim->d_fpre);
+    fl.d_probe_pre = reinterpret_cast<const long long*>(sim->d_fpre) + (n + 1);
+    fl.dry = 0;
+    upload_table<real>(sim);
+    sim->fused_ready = true;
+}
+
 template <typename real>
 cudaError_t launch_one(sj_sim* sim) {
     auto& dv = devv<real>(sim);
     const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
-    if (sim->schedule == SJ_SCHED_FUSED)
-        return launch_fused_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream, 0);
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        prepare_fused<real>(sim);
+        return launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
+    }
     return launch_split_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream);
+}
+
+// Time `steps` dry launches (no state change) of every tiling candidate and
+// keep the fastest: the project's own autotuner for the fused schedule.
+template <typename real>
+void autotune(sj_sim* sim, int steps, int* best_ty, int* best_zs, int* best_ns, float* best_ms) {
+    int nzmax = 1;
+    for (auto& I : devv<real>(sim)) nzmax = std::max(nzmax, I.nz);
+    const int tys[3] = {4, 8, 16};
+    const int zss[4] = {32, 64, 128, nzmax};
+    const int nss[2] = {3, 5};
+    float best = 1e30f;
+    int bty = sim->f_ty, bzs = sim->f_zs, bns = sim->f_ns;
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    ensure_capacity<real>(sim, sim->t + 1);
+    for (int ty : tys)
+        for (int zs : zss)
+            for (int ns : nss) {
+            sim->f_ty = ty;
+            sim->f_zs = zs;
+            sim->f_ns = ns;
+            sim->fused_ready = false;
+            prepare_fused<real>(sim);
+            FusedLaunch fl = sim->fl;
+            fl.dry = 1;
+            const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
+            ck(launch_fused_step<real>(d, sim->n_inst, sim->d_state, fl, sim->stream), "autotune");
+            ck(cudaEventRecord(e0, sim->stream), "event");
+            for (int q = 0; q < steps; ++q)
+                ck(launch_fused_step<real>(d, sim->n_inst, sim->d_state, fl, sim->stream), "autotune");
+            ck(cudaEventRecord(e1, sim->stream), "event");
+            ck(cudaEventSynchronize(e1), "event");
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+            if (ms < best) {
+                best = ms;
+                bty = ty;
+                bzs = zs;
+                bns = ns;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sim->f_ty = bty;
+    sim->f_zs = bzs;
+    sim->f_ns = bns;
+    sim->fused_ready = false;
+    prepare_fused<real>(sim);
+    if (best_ty) *best_ty = bty;
+    if (best_zs) *best_zs = bzs;
+    if (best_ns) *best_ns = bns;
+    if (best_ms) *best_ms = best / steps;
 }
 
 template <typename real>
@@ -676,6 +811,8 @@ template <typename real>
 void do_steps_graph(sj_sim* sim, long long n, int chunk) {
     if (chunk < 1) fail(SJ_E_INVALID, "chunk must be >= 1");
     ensure_capacity<real>(sim, sim->t + n);
+    // everything that allocates or copies happens before the capture
+    if (sim->schedule == SJ_SCHED_FUSED) prepare_fused<real>(sim);
     if (!sim->graph || sim->graph_chunk != chunk || sim->graph_sched != sim->schedule) {
         if (sim->graph) cudaGraphExecDestroy(sim->graph);
         sim->graph = nullptr;
@@ -683,15 +820,20 @@ void do_steps_graph(sj_sim* sim, long long n, int chunk) {
         ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
         cudaStream_t saved = sim->stream;
         sim->stream = cs;
-        cudaGraph_t gr;
+        cudaGraph_t gr = nullptr;
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            for (int q = 0; q < chunk && e == cudaSuccess; ++q) e = launch_one<real>(sim);
+            try {
+                for (int q = 0; q < chunk && e == cudaSuccess; ++q) e = launch_one<real>(sim);
+            } catch (...) {
+                e = cudaErrorStreamCaptureInvalidated;
+            }
             cudaError_t e2 = cudaStreamEndCapture(cs, &gr);
             if (e == cudaSuccess) e = e2;
         }
         sim->stream = saved;
         cudaStreamDestroy(cs);
+        if (e != cudaSuccess && gr) cudaGraphDestroy(gr);
         ck(e, "graph capture");
         e = cudaGraphInstantiate(&sim->graph, gr, 0);
         cudaGraphDestroy(gr);
@@ -859,6 +1001,46 @@ int sj_set_schedule(sj_sim* sim, int32_t schedule) {
         return finish(sim, SJ_E_INVALID, "unknown schedule");
     sim->schedule = schedule;
     return SJ_OK;
+}
+
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t zseg, int32_t ring) {
+    if (!sim) return SJ_E_INVALID;
+    if (tile_y != 4 && tile_y != 8 && tile_y != 16) return finish(sim, SJ_E_INVALID, "tile_y must be 4, 8 or 16");
+    if (zseg < 1) return finish(sim, SJ_E_INVALID, "zseg must be >= 1");
+    if (ring != 3 && ring != 5) return finish(sim, SJ_E_INVALID, "ring must be 3 or 5");
+    sim->f_ty = tile_y;
+    sim->f_zs = zseg;
+    sim->f_ns = ring;
+    sim->fused_ready = false;
+    if (sim->graph) {
+        cudaGraphExecDestroy(sim->graph);
+        sim->graph = nullptr;
+    }
+    return SJ_OK;
+}
+
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* zseg, int32_t* ring) {
+    if (!sim || !tile_y || !zseg || !ring) return SJ_E_INVALID;
+    *tile_y = sim->f_ty;
+    *zseg = sim->f_zs;
+    *ring = sim->f_ns;
+    return SJ_OK;
+}
+
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* zseg, int32_t* ring,
+                float* ms_per_step) {
+    if (!sim || steps < 1) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (sim->graph) {
+        cudaGraphExecDestroy(sim->graph);
+        sim->graph = nullptr;
+    }
+    if (sim->precision == SJ_F64)
+        autotune<double>(sim, steps, tile_y, zseg, ring, ms_per_step);
+    else
+        autotune<float>(sim, steps, tile_y, zseg, ring, ms_per_step);
+    check_status(sim);
+    SJ_CATCH(sim)
 }
 
 int sj_synchronize(sj_sim* sim) {

@@ -67,6 +67,10 @@ struct InstDev {
     double* mon;                // [mon_cap][n_mon]
     long long mon_cap;
     double2* dft;               // [n_dft][n_freq]
+
+    // fused schedule: TMA descriptors and tiling
+    const void* tmap;           // 13 CUtensorMap: E[buffer][c], H[buffer][c], combo
+    int f_ntx, f_nty, f_nzs, f_zs;  // tiles in x, y; z segments and their length
 };
 
 // Step counter and status kept in device memory so that graph replays need
@@ -88,9 +92,24 @@ long long split_block_count_f32(const InstDev<float>& I);
 template <typename real>
 cudaError_t launch_split_step(const InstDev<real>* d_insts, const InstDev<real>* h_insts,
                               int n_inst, DevState* st, cudaStream_t s);
+// Fused schedule launch description (host side).
+struct FusedLaunch {
+    int ty;                     // tile height (4, 8 or 16)
+    int nslot;                  // TMA ring depth (3 or 5 planes)
+    long long n_items;          // stepping blocks (tiles x z segments)
+    long long n_probe_blocks;   // probe blocks after them
+    const long long* d_item_pre;   // [n_inst + 1] prefix of stepping blocks
+    const long long* d_probe_pre;  // [n_inst + 1] prefix of probe blocks
+    int dry;                    // 1 = time only: no step advance, no in-place stores
+};
 template <typename real>
-cudaError_t launch_fused_step(const InstDev<real>* d_insts, const InstDev<real>* h_insts,
-                              int n_inst, DevState* st, cudaStream_t s, int tile_y);
+cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState* st,
+                              const FusedLaunch& fl, cudaStream_t s);
+template <typename real>
+int fused_box_width();          // TMA box width in elements (x)
+template <typename real>
+int fused_box_xoff();           // box starts at i0 - xoff
+int fused_block_threads(int ty);  // threads per block (= probes per probe block)
 template <typename real>
 cudaError_t launch_max_abs_e(const InstDev<real>& h_inst, int buf, double* d_out, cudaStream_t s);
 

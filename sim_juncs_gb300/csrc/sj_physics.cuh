@@ -37,10 +37,12 @@ __device__ __forceinline__ long long slab_idx(const InstDev<real>& I, int a, int
 // curl term of component axis CA (0..2) including the CPML auxiliaries.
 // d1 = difference along A1 = CA+1, d2 = along A2 = CA+2 (mod 3).
 // HALF selects the half-integer profile (H components) or the integer one (E).
-// psi_in/psi_out may alias (in-place schedules).
+// psi_in/psi_out may alias (in-place schedules); store = false recomputes a
+// cell another block owns without writing its auxiliaries.
 template <typename real, int CA, bool HALF>
 __device__ __forceinline__ real curl_psi(const InstDev<real>& I, int i, int j, int k, real d1,
-                                         real d2, real* const* psi_in, real* const* psi_out) {
+                                         real d2, real* const* psi_in, real* const* psi_out,
+                                         bool store = true) {
     constexpr int A1 = (CA + 1) % 3, A2 = (CA + 2) % 3;
     constexpr int P1 = (CA > A1) ? CA - 1 : CA;  // slot of CA in axis A1's pair
     constexpr int P2 = (CA > A2) ? CA - 1 : CA;
@@ -55,7 +57,7 @@ __device__ __forceinline__ real curl_psi(const InstDev<real>& I, int i, int j, i
             const real c = I.prof[A1][(BOFF + 1) * n + q];
             const long long o = (long long)P1 * I.slabvol[A1] + s;
             const real psi = b * psi_in[A1][o] + c * d1;
-            psi_out[A1][o] = psi;
+            if (store) psi_out[A1][o] = psi;
             cur += psi;
         }
     }
@@ -68,7 +70,7 @@ __device__ __forceinline__ real curl_psi(const InstDev<real>& I, int i, int j, i
             const real c = I.prof[A2][(BOFF + 1) * n + q];
             const long long o = (long long)P2 * I.slabvol[A2] + s;
             const real psi = b * psi_in[A2][o] + c * d2;
-            psi_out[A2][o] = psi;
+            if (store) psi_out[A2][o] = psi;
             cur -= psi;
         }
     }
@@ -94,9 +96,10 @@ __device__ __forceinline__ real apply_sources(const InstDev<real>& I, int comp, 
 // E-component finish: sources, polarisation ADE, eps_inf^{-1} scaling.
 template <typename real, int CA>
 __device__ __forceinline__ real e_finish(const InstDev<real>& I, int i, int j, int k, long long n,
-                                         int cb, real e_old, real cur) {
+                                         int cb, real e_old, real cur, bool store = true,
+                                         bool sources = true) {
     real acc = I.S * cur;
-    if (I.n_src) acc = apply_sources(I, CA, i, j, k, n, acc);
+    if (sources && I.n_src) acc = apply_sources(I, CA, i, j, k, n, acc);
     const real* cf = I.coef + (long long)cb * I.ncoef;
     if (I.cflag[cb] & 1) {
         const long long di =
@@ -107,8 +110,10 @@ __device__ __forceinline__ real e_finish(const InstDev<real>& I, int i, int j, i
             const real pn = *pp, pq = *pm;
             const real pnew = I.A[p] * pn + I.B[p] * pq + cf[3 + 3 * p + CA] * e_old;
             acc -= (pnew - pn);
-            *pm = pn;
-            *pp = pnew;
+            if (store) {
+                *pm = pn;
+                *pp = pnew;
+            }
         }
     }
     return e_old + cf[CA] * acc;

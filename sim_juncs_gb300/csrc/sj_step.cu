@@ -18,6 +18,16 @@ __device__ __forceinline__ int find_inst(const long long* __restrict__ blk0, int
     return lo;
 }
 
+// Copy an instance descriptor into shared memory (block-wide, ends with a sync).
+template <typename real>
+__device__ __forceinline__ void load_inst(const InstDev<real>* src, InstDev<real>* dst) {
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    const int nw = (int)(sizeof(InstDev<real>) / sizeof(int));
+    for (int w = threadIdx.y * blockDim.x + threadIdx.x; w < nw; w += blockDim.x * blockDim.y) d[w] = s[w];
+    __syncthreads();
+}
+
 // Last block of the grid advances the device step counter.  Every block of
 // a launch reads `step` before any block can reach this point, so the
 // increment never races with a reader of the same launch.
@@ -91,12 +101,13 @@ k_probe(const InstDev<real>* __restrict__ insts, DevState* st) {
 // Two passes per step over the current buffer, in place: H^{n+1/2} from E^n, then
 // E^{n+1} from H^{n+1/2}.  Block = 32 x 8 threads over (x, y) at one z.
 template <typename real>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_split_h(const InstDev<real>* __restrict__ insts, const long long* __restrict__ blk0, int n_inst,
           DevState* st) {
     const long long b = blockIdx.x;
     const int ii = find_inst(blk0, n_inst, b);
-    const InstDev<real>& I = insts[ii];
+    __shared__ __align__(16) InstDev<real> I;
+    load_inst(insts + ii, &I);
     const long long lb = b - blk0[ii];
     const int bx = (I.nx + 31) >> 5, by = (I.ny + 7) >> 3;
     const int k = (int)(lb / (bx * by));
@@ -105,7 +116,7 @@ k_split_h(const InstDev<real>* __restrict__ insts, const long long* __restrict__
     const int i = (rem % bx) * 32 + threadIdx.x;
     const long long n = st->step;
     if (i >= I.nx || j >= I.ny) return;
-    const int cur = st->cur;
+    const int cur = st->cur;  // (H pass: no block-wide sync after this point)
     const long long o = (long long)k * I.plane + (long long)j * I.px + i;
     const real* Ex = I.F[cur][0];
     const real* Ey = I.F[cur][1];
@@ -140,12 +151,13 @@ k_split_h(const InstDev<real>* __restrict__ insts, const long long* __restrict__
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_split_e(const InstDev<real>* __restrict__ insts, const long long* __restrict__ blk0, int n_inst,
           DevState* st) {
     const long long b = blockIdx.x;
     const int ii = find_inst(blk0, n_inst, b);
-    const InstDev<real>& I = insts[ii];
+    __shared__ __align__(16) InstDev<real> I;
+    load_inst(insts + ii, &I);
     const long long lb = b - blk0[ii];
     const int bx = (I.nx + 31) >> 5, by = (I.ny + 7) >> 3;
     const int k = (int)(lb / (bx * by));

@@ -70,6 +70,22 @@ class Fields:
     def set_schedule(self, schedule):
         self._ck(self.lib.sj_set_schedule(self.handle, _SCHED[schedule]))
 
+    def set_tiling(self, tile_y, zseg, ring=5):
+        self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(zseg), int(ring)))
+
+    def tiling(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._ck(self.lib.sj_get_tiling(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def autotune(self, steps=3):
+        """Pick the fused tiling by timing state-preserving launches.
+        Returns (tile_y, zseg, ring, ms_per_step)."""
+        a, b, c, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
+        self._ck(self.lib.sj_autotune(self.handle, int(steps), C.byref(a), C.byref(b), C.byref(c),
+                                      C.byref(ms)))
+        return a.value, b.value, c.value, ms.value
+
     def synchronize(self):
         self._ck(self.lib.sj_synchronize(self.handle))
 

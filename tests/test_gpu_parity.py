@@ -1,8 +1,10 @@
 """Parity of the CUDA stepper with the FP64 CPU oracle, through the C ABI.
 
-Bar: FP64 fields, monitors and DFT sums within 1e-10 of the oracle,
-relative to the largest magnitude of the compared quantity; FP32 gap
-monitors within 1e-4 of FP64 (the target for the FP32 path).
+Bar: FP64 fields within 1e-10 of the oracle relative to the largest field
+magnitude the run has reached so far (a pulse that has decayed 1e6-fold in
+the PML carries the absolute rounding of its peak); FP64 monitor series and
+DFT sums within 1e-10 relative to their own maximum; FP32 gap monitors and
+DFTs within 1e-4 of FP64 (the target for the FP32 path).
 """
 import numpy as np
 import pytest
@@ -24,11 +26,19 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a)))
 
 
-def compare_fields(f, o, tol, inst=0):
+def compare_fields(f, o, tol, inst=0, peak=0.0):
+    """Every component within tol of the oracle, relative to the largest
+    field magnitude over all six components and over the run so far (`peak`;
+    a component that symmetry keeps at roundoff level has no meaningful
+    relative error of its own).  Returns the updated peak."""
+    gs = [f.get_array(c, inst) for c in range(6)]
+    rs = [o.get_array(c) for c in range(6)]
+    scale = max([peak] + [float(np.max(np.abs(r))) for r in rs])
+    assert scale > 0
     for c in range(6):
-        g = f.get_array(c, inst)
-        r = o.get_array(c)
-        assert rel(g, r) <= tol, (c, rel(g, r))
+        err = float(np.max(np.abs(gs[c] - rs[c]))) / scale
+        assert err <= tol, (c, err)
+    return scale
 
 
 @pytest.mark.parametrize("schedule", ["split", "fused"])
@@ -36,11 +46,12 @@ def test_junction_f64_matches_oracle(lib, oracle_lib, schedule):
     inst = junction_instance()            # 64^3, 20 px/um, 2000 steps
     f = Fields(inst, "f64", schedule)
     o = OracleFields(inst)
+    peak = 0.0
     for upto in (1, 10, 400, 2000):
         n = upto - o.steps_done
         f.step(n)
         o.step(n)
-        compare_fields(f, o, TOL64)
+        peak = compare_fields(f, o, TOL64, peak=peak)
     assert f.steps_done == 2000
     mg, mo = f.monitors(), o.monitors()
     assert mg.shape == mo.shape == (8, 100)
@@ -112,14 +123,51 @@ def test_graph_replay_matches_plain_launches(lib, schedule):
     np.testing.assert_array_equal(a.monitors(), b.monitors())
 
 
-def test_fused_and_split_agree_bitwise_f64(lib):
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_fused_and_split_agree(lib, precision, tol):
+    # same per-voxel formulas, different data staging and instruction
+    # selection (fused multiply-adds may contract differently)
     inst = junction_instance(n=48, res=15.0)
-    a = Fields(inst, "f64", "split")
-    b = Fields(inst, "f64", "fused")
+    a = Fields(inst, precision, "split")
+    b = Fields(inst, precision, "fused")
     a.step(137)
     b.step(137)
+    scale = max(float(np.max(np.abs(a.get_array(c)))) for c in range(6))
     for c in range(6):
-        assert rel(b.get_array(c), a.get_array(c)) <= 1e-13
+        assert float(np.max(np.abs(b.get_array(c) - a.get_array(c)))) <= tol * scale, c
+    assert rel(b.monitors(), a.monitors()) <= tol
+
+
+@pytest.mark.parametrize("ty,zs,ring", [(4, 7, 3), (16, 13, 5), (8, 1000, 3), (4, 45, 5)])
+def test_fused_tilings_agree(lib, ty, zs, ring):
+    # tile heights, z-segment lengths (incl. ragged ones) and ring depths
+    # change only the work decomposition, never the numbers
+    inst = junction_instance(n=45, res=14.0)
+    a = Fields(inst, "f32", "fused")
+    b = Fields(inst, "f32", "fused")
+    a.set_tiling(8, 64, 5)
+    b.set_tiling(ty, zs, ring)
+    a.step(60)
+    b.step(60)
+    for c in range(6):
+        np.testing.assert_array_equal(b.get_array(c), a.get_array(c))
+    np.testing.assert_array_equal(b.monitors(), a.monitors())
+
+
+def test_autotune_leaves_state_untouched(lib):
+    inst = junction_instance(n=40, res=12.5)
+    a = Fields(inst, "f32", "fused")
+    b = Fields(inst, "f32", "fused")
+    a.step(50)
+    b.step(50)
+    ty, zs, ring, ms = b.autotune(steps=2)
+    assert ty in (4, 8, 16) and zs >= 1 and ring in (3, 5) and ms > 0
+    assert b.steps_done == 50
+    a.step(50)
+    b.step(50)
+    for c in range(6):
+        np.testing.assert_array_equal(b.get_array(c), a.get_array(c))
+    np.testing.assert_array_equal(b.monitors(), a.monitors())
 
 
 def test_write_read_roundtrip_and_queries(lib):
