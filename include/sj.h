@@ -310,6 +310,25 @@ int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out);
    point (composite_object::in, src/cgs.cpp:403-449). */
 int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out_masks);
 
+/* Allocation-free rasteriser (no counterpart in the reference).
+   For callers that cannot allocate device memory: code running while a
+   stream is being captured into a CUDA graph (cudaMalloc is not capturable),
+   or hosts whose device memory comes from their own pool.  Same result as
+   sj_rasterize, but the caller passes the output as a DEVICE buffer
+   d_out_masks[3][nz][ny][nx] and the work is queued on `stream` (a
+   cudaStream_t; NULL = the legacy default stream) without waiting for it.
+   The flattened CSG program is staged in one library-owned static device
+   array of SJ_RASTER_STATIC_NODES nodes in total, which every GPU that loads
+   the library holds until exit; larger scenes are rejected with SJ_E_RANGE.
+   The first call on a device looks up that array's address (once per
+   device) and must come before any stream capture.  All calls share the
+   array and it keeps the last call's program: calls that overlap on the GPU
+   (e.g. on two streams) race.  No cudaMalloc, cudaFree or other allocating
+   routine is called. */
+#define SJ_RASTER_STATIC_NODES 512
+int sj_rasterize_static(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* d_out_masks,
+                        void* stream);
+
 /* ---------------------------------------------------------------- host helpers */
 /* gaussian_src_time_phase::dipole (src/disp.cpp:378-400) / meep's
    continuous_src_time, and the current the stepper injects at time t */

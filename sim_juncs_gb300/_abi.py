@@ -26,6 +26,7 @@ PROBE_MONITOR, PROBE_DFT = 1, 2
 CSG_BOX, CSG_SPHERE, CSG_CYLINDER, CSG_PLANE = 0, 1, 2, 3
 CSG_UNION, CSG_INTERSECT, CSG_PASS, CSG_CONST, CSG_NOOP = 4, 5, 6, 7, 8
 MAX_POLES, MAX_SOURCES, MAX_REGIONS = 8, 4, 8
+RASTER_STATIC_NODES = 512
 EPS_SUM, EPS_FIRST = 0, 1
 
 
@@ -126,6 +127,7 @@ SIGNATURES = {
     "sj_read_class_map": (C.c_int, [_P, C.c_int32, _U8, C.c_size_t]),
     "sj_max_abs_e": (C.c_int, [_P, C.c_int32, _D]),
     "sj_rasterize": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _U8]),
+    "sj_rasterize_static": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _P, _P]),
     "sj_source_dipole": (C.c_int, [C.POINTER(SourceDesc), C.c_double, _D, _D]),
     "sj_source_current": (C.c_int, [C.POINTER(SourceDesc), C.c_double, C.c_double, _D, _D]),
     "sj_source_last_time": (C.c_double, [C.POINTER(SourceDesc)]),

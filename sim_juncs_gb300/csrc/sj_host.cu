@@ -1214,6 +1214,14 @@ int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* 
     return SJ_OK;
 }
 
+int sj_rasterize_static(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* d_out_masks,
+                        void* stream) {
+    const char* msg = "";
+    const int rc = rasterize_static(grid, scene, d_out_masks, static_cast<cudaStream_t>(stream), &msg);
+    if (rc != SJ_OK) return finish(nullptr, rc, msg);
+    return SJ_OK;
+}
+
 int sj_source_dipole(const sj_source_desc* src, double t, double* re, double* im) {
     if (!src || !re || !im) return SJ_E_INVALID;
     const std::complex<double> v = dipole(*src, t);

@@ -125,6 +125,8 @@ cudaError_t launch_combo_assign(const uint8_t* d_cls, long long cpitch, int nx, 
                                 cudaStream_t s);
 cudaError_t launch_combo_hist(const uint8_t* d_combo, int nx, int ny, int nz, int px,
                               unsigned long long* d_hist, cudaStream_t s);
+int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_out, cudaStream_t s,
+                     const char** msg);
 cudaError_t launch_disp_bbox(const uint8_t* d_combo, const uint8_t* d_cflag, int nx, int ny,
                              int nz, int px, int* d_box, cudaStream_t s);
 

@@ -230,3 +230,121 @@ cudaError_t launch_combo_hist(const uint8_t* d_combo, int nx, int ny, int nz, in
     return cudaGetLastError();
 }
 }  // namespace sj
+
+// ---------------------------------------------------------------------------
+// Allocation-free rasteriser (sj_rasterize_static).
+//
+// The region start table and the concatenated CSG programs live in one
+// file-scope device array instead of cudaMalloc'd buffers.  Host code never
+// names the array directly: its device address comes from
+// cudaGetSymbolAddress, looked up once per device with that device current.
+#include <mutex>
+
+namespace sj {
+
+constexpr size_t RASTER_TABLE_BYTES = 64;  // int start[SJ_MAX_REGIONS + 1], padded
+constexpr size_t RASTER_SCRATCH_BYTES =
+    RASTER_TABLE_BYTES + (size_t)SJ_RASTER_STATIC_NODES * sizeof(sj_csg_node);
+static_assert((SJ_MAX_REGIONS + 1) * sizeof(int) <= RASTER_TABLE_BYTES, "region table too small");
+
+static __device__ __align__(256) unsigned char g_raster_scratch[RASTER_SCRATCH_BYTES];
+
+namespace {
+constexpr int MAX_DEVICES = 64;
+std::mutex g_scratch_mu;
+unsigned char* g_scratch_ptr[MAX_DEVICES] = {};
+
+// Device address of g_raster_scratch on the current device.
+cudaError_t raster_scratch(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_raster_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+// Returns 0 or an SJ_E_* code; *msg gets a static description on failure.
+int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_out, cudaStream_t s,
+                     const char** msg) {
+    if (!g || !sc || !d_out) {
+        *msg = "NULL argument";
+        return SJ_E_INVALID;
+    }
+    if (g->nx < 1 || g->ny < 1 || g->nz < 1 || !(g->dx > 0)) {
+        *msg = "bad grid";
+        return SJ_E_INVALID;
+    }
+    if (sc->n_regions < 0 || sc->n_regions > SJ_MAX_REGIONS || (sc->n_regions > 0 && !sc->regions)) {
+        *msg = "scene n_regions must be in [0, 8]";
+        return SJ_E_INVALID;
+    }
+    int start[SJ_MAX_REGIONS + 1] = {0};
+    for (int r = 0; r < sc->n_regions; ++r) {
+        const sj_region_desc& rg = sc->regions[r];
+        if (rg.n_nodes < 1 || !rg.nodes) {
+            *msg = "region without CSG nodes";
+            return SJ_E_INVALID;
+        }
+        int depth = 0;
+        for (int q = 0; q < rg.n_nodes; ++q) {
+            const int op = rg.nodes[q].op;
+            if (op < 0 || op > SJ_CSG_NOOP) {
+                *msg = "unknown CSG op";
+                return SJ_E_INVALID;
+            }
+            if (op <= SJ_CSG_PLANE || op == SJ_CSG_CONST || op == SJ_CSG_NOOP)
+                ++depth;
+            else if (op == SJ_CSG_UNION || op == SJ_CSG_INTERSECT)
+                depth = depth >= 2 ? depth - 1 : -1000;
+            else if (depth < 1)
+                depth = -1000;
+            if (depth < 0 || depth > 64) {
+                *msg = "malformed CSG program";
+                return SJ_E_INVALID;
+            }
+        }
+        if (depth != 1) {
+            *msg = "CSG program must leave exactly one value";
+            return SJ_E_INVALID;
+        }
+        if (start[r] + rg.n_nodes > SJ_RASTER_STATIC_NODES) {
+            *msg = "scene has more CSG nodes than SJ_RASTER_STATIC_NODES (512)";
+            return SJ_E_RANGE;
+        }
+        start[r + 1] = start[r] + rg.n_nodes;
+    }
+    unsigned char* base = nullptr;
+    cudaError_t e = raster_scratch(&base);
+    if (e != cudaSuccess) {
+        *msg = "cudaGetSymbolAddress of the rasteriser scratch array failed";
+        return SJ_E_CUDA;
+    }
+    // the program is overwritten in full by every call; nothing needs clearing
+    sj_csg_node* d_nodes = reinterpret_cast<sj_csg_node*>(base + RASTER_TABLE_BYTES);
+    int* d_start = reinterpret_cast<int*>(base);
+    e = cudaMemcpyAsync(d_start, start, sizeof(start), cudaMemcpyHostToDevice, s);
+    for (int r = 0; r < sc->n_regions && e == cudaSuccess; ++r)
+        e = cudaMemcpyAsync(d_nodes + start[r], sc->regions[r].nodes,
+                            (size_t)sc->regions[r].n_nodes * sizeof(sj_csg_node), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        const long long nv = (long long)g->nx * g->ny * g->nz;
+        e = launch_rasterize(d_nodes, d_start, sc->n_regions, g->nx, g->ny, g->nz, g->dx, g->origin, d_out,
+                             nv, g->nx, s);
+    }
+    if (e != cudaSuccess) {
+        *msg = "CUDA call failed in sj_rasterize_static";
+        return SJ_E_CUDA;
+    }
+    return SJ_OK;
+}
+
+}  // namespace sj
