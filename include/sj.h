@@ -62,7 +62,8 @@ enum { SJ_EX = 0, SJ_EY = 1, SJ_EZ = 2, SJ_HX = 3, SJ_HY = 4, SJ_HZ = 5 };
 enum { SJ_F64 = 0, SJ_F32 = 1 };
 
 /* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel, SPLIT the
-   two-pass (H then E) reference schedule kept for cross-checking */
+   two-pass (H then E) schedule.  Default: FUSED for SJ_F32 (HBM-bound),
+   SPLIT for SJ_F64 (bound by FP64 arithmetic, where SPLIT does less work) */
 enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1 };
 
 #define SJ_MAX_POLES 8
@@ -254,14 +255,14 @@ int sj_set_stream(sj_sim* sim, void* cuda_stream);
 int sj_set_schedule(sj_sim* sim, int32_t schedule);
 int sj_synchronize(sj_sim* sim);
 
-/* fused-schedule tiling: tile_y in {4, 8, 16} rows per block, z segments of
-   zseg planes (each block marches one segment), TMA ring of `ring` planes
-   (3 or 5) */
-int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t zseg, int32_t ring);
-int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* zseg, int32_t* ring);
-/* time every tiling candidate with `steps` launches that leave the state
+/* fused-schedule tiling: tiles of 32 x tile_y cells, `rows` consecutive rows
+   per thread ((tile_y, rows) in {(4,1), (8,1), (16,1), (8,2), (16,2)}),
+   z segments of zseg planes (each block marches one segment) */
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t rows, int32_t zseg);
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* rows, int32_t* zseg);
+/* time every fused tiling with `steps` launches that leave the state
    untouched, keep the fastest and report it (any output may be NULL) */
-int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* zseg, int32_t* ring,
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* rows, int32_t* zseg,
                 float* ms_per_step);
 
 /* ---------------------------------------------------------------- stepping */

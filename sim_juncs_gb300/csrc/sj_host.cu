@@ -140,7 +140,7 @@ struct sj_sim {
     int graph_chunk = 0;
     int graph_sched = -1;
     // fused schedule: tiling, tensor maps, block prefixes
-    int f_ty = 8, f_zs = 64, f_ns = 5;
+    int f_ty = 8, f_zs = 64, f_rows = 1;
     bool fused_ready = false;
     FusedLaunch fl{};
     void* d_fpre = nullptr;
@@ -472,11 +472,10 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
         I.pl[a] = pl, I.ph[a] = ph;
         I.prof[a] = sim->upload(prof);
         const long long w = pl + ph;
-        I.slabvol[a] = a == 0 ? (long long)nz * ny * w : (a == 1 ? (long long)nz * w * px : w * (long long)ny * px);
-        if (w > 0) {
-            I.psiE[a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
-            I.psiH[0][a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
-            I.psiH[1][a] = (real*)sim->dalloc(2 * I.slabvol[a] * sizeof(real));
+        if (w > 0) {  // full-grid layout; only the slab voxels are ever touched
+            I.psiE[a] = (real*)sim->dalloc(2 * vol * sizeof(real));
+            I.psiH[0][a] = (real*)sim->dalloc(2 * vol * sizeof(real));
+            I.psiH[1][a] = (real*)sim->dalloc(2 * vol * sizeof(real));
         }
         const long long slab_vox = a == 0 ? (long long)nz * ny * w : (a == 1 ? (long long)nz * w * nx : w * (long long)ny * nx);
         H.bytes_per_step += (double)slab_vox * 4 * 2 * sizeof(real);
@@ -684,9 +683,10 @@ void prepare_fused(sj_sim* sim) {
     auto& dv = devv<real>(sim);
     const int n = sim->n_inst, ty = sim->f_ty;
     auto encode = tensor_map_encoder();
-    std::vector<CUtensorMap> maps((size_t)n * 13);
+    const int nmaps = fused_tensor_maps();
+    std::vector<CUtensorMap> maps((size_t)n * nmaps);
     std::vector<long long> pre(2 * (n + 1), 0);
-    const int thr = fused_block_threads(ty);
+    const int thr = fused_block_threads(ty, sim->f_rows);
     for (int q = 0; q < n; ++q) {
         InstDev<real>& I = dv[q];
         const cuuint64_t dims[3] = {(cuuint64_t)I.nx, (cuuint64_t)I.ny, (cuuint64_t)I.nz};
@@ -703,13 +703,25 @@ void prepare_fused(sj_sim* sim) {
         const CUtensorMapDataType fdt =
             sizeof(real) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         const cuuint32_t bx = (cuuint32_t)fused_box_width<real>();
-        CUtensorMap* m = &maps[(size_t)q * 13];
+        // slots: [0..5] E[b][c] (halo box), [6..11] H[b][c] (halo box), [12] combo (own box),
+        // [13..18] psi_E[a][pair] (own box), [19..30] psi_H[b][a][pair] (halo box)
+        CUtensorMap* m = &maps[(size_t)q * nmaps];
         for (int b = 0; b < 2; ++b)
             for (int c = 0; c < 3; ++c) {
                 enc(m + b * 3 + c, fdt, I.F[b][c], sizeof(real), bx, (cuuint32_t)(ty + 2));      // E
                 enc(m + 6 + b * 3 + c, fdt, I.F[b][3 + c], sizeof(real), bx, (cuuint32_t)(ty + 1));  // H
             }
         enc(m + 12, CU_TENSOR_MAP_DATA_TYPE_UINT8, const_cast<uint8_t*>(I.combo), 1, 32, (cuuint32_t)ty);
+        for (int a = 0; a < 3; ++a)
+            for (int pp = 0; pp < 2; ++pp) {
+                // axes without a slab never issue these loads; encode a valid placeholder
+                real* pe = I.psiE[a] ? I.psiE[a] + (size_t)pp * I.vol : I.F[0][0];
+                enc(m + 13 + a * 2 + pp, fdt, pe, sizeof(real), 32, (cuuint32_t)ty);
+                for (int b = 0; b < 2; ++b) {
+                    real* ph = I.psiH[b][a] ? I.psiH[b][a] + (size_t)pp * I.vol : I.F[0][3];
+                    enc(m + 19 + b * 6 + a * 2 + pp, fdt, ph, sizeof(real), bx, (cuuint32_t)(ty + 1));
+                }
+            }
         I.f_ntx = (I.nx + 31) / 32;
         I.f_nty = (I.ny + ty - 1) / ty;
         I.f_zs = std::max(1, std::min(sim->f_zs, I.nz));
@@ -721,10 +733,10 @@ void prepare_fused(sj_sim* sim) {
     sim->dfree(sim->d_fpre);
     sim->d_tmaps = sim->upload(maps);
     sim->d_fpre = sim->upload(pre);
-    for (int q = 0; q < n; ++q) dv[q].tmap = reinterpret_cast<const CUtensorMap*>(sim->d_tmaps) + (size_t)q * 13;
+    for (int q = 0; q < n; ++q) dv[q].tmap = reinterpret_cast<const CUtensorMap*>(sim->d_tmaps) + (size_t)q * nmaps;
     FusedLaunch& fl = sim->fl;
     fl.ty = ty;
-    fl.nslot = sim->f_ns;
+    fl.rows = sim->f_rows;
     fl.n_items = pre[n];
     fl.n_probe_blocks = pre[2 * n + 1];
     fl.d_item_pre = reinterpret_cast<const long long*>(sim->d_fpre);
@@ -748,24 +760,25 @@ cudaError_t launch_one(sj_sim* sim) {
 // Time `steps` dry launches (no state change) of every tiling candidate and
 // keep the fastest: the project's own autotuner for the fused schedule.
 template <typename real>
-void autotune(sj_sim* sim, int steps, int* best_ty, int* best_zs, int* best_ns, float* best_ms) {
+void autotune(sj_sim* sim, int steps, int* best_ty, int* best_rows, int* best_zs, float* best_ms) {
     int nzmax = 1;
     for (auto& I : devv<real>(sim)) nzmax = std::max(nzmax, I.nz);
-    const int tys[3] = {4, 8, 16};
-    const int zss[4] = {32, 64, 128, nzmax};
-    const int nss[2] = {3, 5};
+    const int tilings[5][2] = {{4, 1}, {8, 1}, {16, 1}, {8, 2}, {16, 2}};
+    const int zss[3] = {32, 64, nzmax};
     float best = 1e30f;
-    int bty = sim->f_ty, bzs = sim->f_zs, bns = sim->f_ns;
+    int bty = sim->f_ty, bzs = sim->f_zs, brows = sim->f_rows;
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     ensure_capacity<real>(sim, sim->t + 1);
-    for (int ty : tys)
-        for (int zs : zss)
-            for (int ns : nss) {
+    for (const auto& tl : tilings)
+        for (int zs : zss) {
+            const int ty = tl[0], rows = tl[1];
+            const int sb = fused_smem_bytes<real>(ty, rows);
+            if (sb < 0 || sb > FUSED_MAX_SMEM) continue;  // does not fit one SM
             sim->f_ty = ty;
             sim->f_zs = zs;
-            sim->f_ns = ns;
+            sim->f_rows = rows;
             sim->fused_ready = false;
             prepare_fused<real>(sim);
             FusedLaunch fl = sim->fl;
@@ -783,19 +796,19 @@ void autotune(sj_sim* sim, int steps, int* best_ty, int* best_zs, int* best_ns, 
                 best = ms;
                 bty = ty;
                 bzs = zs;
-                bns = ns;
+                brows = rows;
             }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     sim->f_ty = bty;
     sim->f_zs = bzs;
-    sim->f_ns = bns;
+    sim->f_rows = brows;
     sim->fused_ready = false;
     prepare_fused<real>(sim);
     if (best_ty) *best_ty = bty;
     if (best_zs) *best_zs = bzs;
-    if (best_ns) *best_ns = bns;
+    if (best_rows) *best_rows = brows;
     if (best_ms) *best_ms = best / steps;
 }
 
@@ -953,6 +966,9 @@ int sj_batch_create(int32_t n, const sj_instance_desc* insts, int32_t precision,
     try {
         sim->precision = precision;
         sim->n_inst = n;
+        // FP32 fields are HBM-bound: one fused pass; FP64 arithmetic is bound by
+        // the FP64 pipe, where the split schedule's fewer operations win
+        sim->schedule = precision == SJ_F32 ? SJ_SCHED_FUSED : SJ_SCHED_SPLIT;
         ck(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "stream create");
         sim->own_stream = true;
         sim->d_state = (DevState*)sim->dalloc(sizeof(DevState));
@@ -1003,14 +1019,16 @@ int sj_set_schedule(sj_sim* sim, int32_t schedule) {
     return SJ_OK;
 }
 
-int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t zseg, int32_t ring) {
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t rows, int32_t zseg) {
     if (!sim) return SJ_E_INVALID;
-    if (tile_y != 4 && tile_y != 8 && tile_y != 16) return finish(sim, SJ_E_INVALID, "tile_y must be 4, 8 or 16");
+    const int sb = sim->precision == SJ_F64 ? fused_smem_bytes<double>(tile_y, rows)
+                                            : fused_smem_bytes<float>(tile_y, rows);
+    if (sb < 0) return finish(sim, SJ_E_INVALID, "unsupported tiling (tile_y, rows)");
+    if (sb > FUSED_MAX_SMEM) return finish(sim, SJ_E_INVALID, "tiling needs more shared memory than one SM has");
     if (zseg < 1) return finish(sim, SJ_E_INVALID, "zseg must be >= 1");
-    if (ring != 3 && ring != 5) return finish(sim, SJ_E_INVALID, "ring must be 3 or 5");
     sim->f_ty = tile_y;
+    sim->f_rows = rows;
     sim->f_zs = zseg;
-    sim->f_ns = ring;
     sim->fused_ready = false;
     if (sim->graph) {
         cudaGraphExecDestroy(sim->graph);
@@ -1019,15 +1037,15 @@ int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t zseg, int32_t ring) {
     return SJ_OK;
 }
 
-int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* zseg, int32_t* ring) {
-    if (!sim || !tile_y || !zseg || !ring) return SJ_E_INVALID;
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* rows, int32_t* zseg) {
+    if (!sim || !tile_y || !rows || !zseg) return SJ_E_INVALID;
     *tile_y = sim->f_ty;
+    *rows = sim->f_rows;
     *zseg = sim->f_zs;
-    *ring = sim->f_ns;
     return SJ_OK;
 }
 
-int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* zseg, int32_t* ring,
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* rows, int32_t* zseg,
                 float* ms_per_step) {
     if (!sim || steps < 1) return SJ_E_INVALID;
     SJ_TRY(sim)
@@ -1036,9 +1054,9 @@ int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* zseg, int3
         sim->graph = nullptr;
     }
     if (sim->precision == SJ_F64)
-        autotune<double>(sim, steps, tile_y, zseg, ring, ms_per_step);
+        autotune<double>(sim, steps, tile_y, rows, zseg, ms_per_step);
     else
-        autotune<float>(sim, steps, tile_y, zseg, ring, ms_per_step);
+        autotune<float>(sim, steps, tile_y, rows, zseg, ms_per_step);
     check_status(sim);
     SJ_CATCH(sim)
 }

@@ -46,12 +46,14 @@ struct InstDev {
     long long dvol;
     real* P;                    // [n_poles][2 levels: n, n-1][3 comps][dvol]
 
-    // CPML: slab thickness (cells) per axis and face, profiles, psi storage
+    // CPML: slab thickness (cells) per axis and face, profiles, psi storage.
+    // psi arrays share the field layout ([nz][ny][px] per component) so a
+    // voxel's psi sits at the same offset as its fields; only axes with a
+    // slab allocate them, and only slab voxels are ever read or written.
     int pl[3], ph[3];
     const real* prof[3];        // per axis: b_int[n], c_int[n], b_half[n], c_half[n]
-    long long slabvol[3];
-    real* psiE[3];              // per axis: [2 comps][slabvol]
-    real* psiH[2][3];           // [ping-pong][axis]: [2 comps][slabvol]
+    real* psiE[3];              // per axis: [2 comps][vol]
+    real* psiH[2][3];           // [ping-pong][axis]: [2 comps][vol]
 
     int n_src;
     SrcDev<real> src[MAXS];
@@ -69,7 +71,7 @@ struct InstDev {
     double2* dft;               // [n_dft][n_freq]
 
     // fused schedule: TMA descriptors and tiling
-    const void* tmap;           // 13 CUtensorMap: E[buffer][c], H[buffer][c], combo
+    const void* tmap;           // 31 CUtensorMap: E[b][c], H[b][c], combo, psiE[a][p], psiH[b][a][p]
     int f_ntx, f_nty, f_nzs, f_zs;  // tiles in x, y; z segments and their length
 };
 
@@ -94,8 +96,8 @@ cudaError_t launch_split_step(const InstDev<real>* d_insts, const InstDev<real>*
                               int n_inst, DevState* st, cudaStream_t s);
 // Fused schedule launch description (host side).
 struct FusedLaunch {
-    int ty;                     // tile height (4, 8 or 16)
-    int nslot;                  // TMA ring depth (3 or 5 planes)
+    int ty;                     // tile height (4, 8 or 16 rows)
+    int rows;                   // rows per thread (2 or 4)
     long long n_items;          // stepping blocks (tiles x z segments)
     long long n_probe_blocks;   // probe blocks after them
     const long long* d_item_pre;   // [n_inst + 1] prefix of stepping blocks
@@ -109,7 +111,11 @@ template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>
 int fused_box_xoff();           // box starts at i0 - xoff
-int fused_block_threads(int ty);  // threads per block (= probes per probe block)
+int fused_block_threads(int ty, int rows);  // threads per block (= probes per probe block)
+int fused_tensor_maps();          // CUtensorMap slots per instance
+template <typename real>
+int fused_smem_bytes(int ty, int rows);  // dynamic shared memory of a tiling, -1 if unsupported
+constexpr int FUSED_MAX_SMEM = 227 * 1024;
 template <typename real>
 cudaError_t launch_max_abs_e(const InstDev<real>& h_inst, int buf, double* d_out, cudaStream_t s);
 

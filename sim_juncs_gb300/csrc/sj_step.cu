@@ -131,19 +131,19 @@ k_split_h(const InstDev<real>* __restrict__ insts, const long long* __restrict__
     const real ez_i = xi ? Ez[o + 1] : real(0), ez_j = yj ? Ez[o + I.px] : real(0);
     real* const* psi = I.psiH[cur];
     {
-        const real cv = curl_psi<real, 0, true>(I, i, j, k, ez_j - ez, ey_k - ey, psi, psi);
+        const real cv = curl_psi<real, 0, true>(I, i, j, k, o, ez_j - ez, ey_k - ey, psi, psi);
         real acc = -(I.S * cv);
         if (I.n_src) acc = apply_sources(I, SJ_HX, i, j, k, n, acc);
         Hx[o] = Hx[o] + acc;
     }
     {
-        const real cv = curl_psi<real, 1, true>(I, i, j, k, ex_k - ex, ez_i - ez, psi, psi);
+        const real cv = curl_psi<real, 1, true>(I, i, j, k, o, ex_k - ex, ez_i - ez, psi, psi);
         real acc = -(I.S * cv);
         if (I.n_src) acc = apply_sources(I, SJ_HY, i, j, k, n, acc);
         Hy[o] = Hy[o] + acc;
     }
     {
-        const real cv = curl_psi<real, 2, true>(I, i, j, k, ey_i - ey, ex_j - ex, psi, psi);
+        const real cv = curl_psi<real, 2, true>(I, i, j, k, o, ey_i - ey, ex_j - ex, psi, psi);
         real acc = -(I.S * cv);
         if (I.n_src) acc = apply_sources(I, SJ_HZ, i, j, k, n, acc);
         Hz[o] = Hz[o] + acc;
@@ -181,15 +181,15 @@ k_split_e(const InstDev<real>* __restrict__ insts, const long long* __restrict__
         const int cb = I.combo[o];
         real* const* psi = I.psiE;
         {
-            const real cv = curl_psi<real, 0, false>(I, i, j, k, hz - hz_j, hy - hy_k, psi, psi);
+            const real cv = curl_psi<real, 0, false>(I, i, j, k, o, hz - hz_j, hy - hy_k, psi, psi);
             Ex[o] = e_finish<real, 0>(I, i, j, k, n, cb, Ex[o], cv);
         }
         {
-            const real cv = curl_psi<real, 1, false>(I, i, j, k, hx - hx_k, hz - hz_i, psi, psi);
+            const real cv = curl_psi<real, 1, false>(I, i, j, k, o, hx - hx_k, hz - hz_i, psi, psi);
             Ey[o] = e_finish<real, 1>(I, i, j, k, n, cb, Ey[o], cv);
         }
         {
-            const real cv = curl_psi<real, 2, false>(I, i, j, k, hy - hy_i, hx - hx_j, psi, psi);
+            const real cv = curl_psi<real, 2, false>(I, i, j, k, o, hy - hy_i, hx - hx_j, psi, psi);
             Ez[o] = e_finish<real, 2>(I, i, j, k, n, cb, Ez[o], cv);
         }
     }

@@ -20,7 +20,7 @@ _SCHED = {"fused": _abi.SCHED_FUSED, "split": _abi.SCHED_SPLIT,
 class Fields:
     """One or many simulation instances stepped by the CUDA library."""
 
-    def __init__(self, instances, precision="f64", schedule="fused", stream=None):
+    def __init__(self, instances, precision="f64", schedule=None, stream=None):
         self.lib = _abi.load_library()
         if isinstance(instances, Instance):
             instances = [instances]
@@ -37,7 +37,8 @@ class Fields:
         _abi.check(self.lib, self.lib.sj_batch_create(n, descs, self.precision, C.byref(handle)))
         self.handle = handle
         self._holders = None  # the library copied everything it needs
-        self.set_schedule(schedule)
+        if schedule is not None:  # default: fused for f32, split for f64
+            self.set_schedule(schedule)
         if stream is not None:
             self.set_stream(stream)
 
@@ -70,8 +71,9 @@ class Fields:
     def set_schedule(self, schedule):
         self._ck(self.lib.sj_set_schedule(self.handle, _SCHED[schedule]))
 
-    def set_tiling(self, tile_y, zseg, ring=5):
-        self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(zseg), int(ring)))
+    def set_tiling(self, tile_y, rows, zseg):
+        """Fused-schedule tiling: 32 x tile_y tiles, `rows` rows per thread, z segments."""
+        self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(rows), int(zseg)))
 
     def tiling(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
@@ -80,7 +82,7 @@ class Fields:
 
     def autotune(self, steps=3):
         """Pick the fused tiling by timing state-preserving launches.
-        Returns (tile_y, zseg, ring, ms_per_step)."""
+        Returns (tile_y, rows, zseg, ms_per_step)."""
         a, b, c, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
         self._ck(self.lib.sj_autotune(self.handle, int(steps), C.byref(a), C.byref(b), C.byref(c),
                                       C.byref(ms)))
