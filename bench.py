@@ -161,8 +161,8 @@ def run_ours(args):
     insts, cfg = workload_instances(args.workload, rank)
     f = Fields(insts, "f32", args.schedule, stream=torch.cuda.current_stream())
     if args.schedule == "fused":
-        ty, rows, zs, _ = f.autotune(steps=2)
-        cfg = dict(cfg, tile=f"32x{ty}", rows_per_thread=rows, zseg=zs, tiling="autotuned")
+        ty, ring, zs, _ = f.autotune(steps=2)
+        cfg = dict(cfg, tile=f"32x{ty}", tma_ring=ring, zseg=zs, tiling="autotuned")
     has_probes = any(i.probes for i in insts)
     lps = (1 if args.schedule == "fused" else 2) + (1 if has_probes and args.schedule == "split" else 0)
     voxels = f.voxels()

@@ -61,10 +61,13 @@ enum { SJ_EX = 0, SJ_EY = 1, SJ_EZ = 2, SJ_HX = 3, SJ_HY = 4, SJ_HZ = 5 };
    monitor sums are always FP64 */
 enum { SJ_F64 = 0, SJ_F32 = 1 };
 
-/* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel, SPLIT the
-   two-pass (H then E) schedule.  Default: FUSED for SJ_F32 (HBM-bound),
-   SPLIT for SJ_F64 (bound by FP64 arithmetic, where SPLIT does less work) */
-enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1 };
+/* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel (one thread
+   per (i,j) column marching z, neighbour H recomputed, no shared memory);
+   SPLIT the two-pass (H then E) schedule; TMA the single-pass kernel that
+   stages tiles through a TMA/mbarrier shared-memory ring.  Default: FUSED for
+   SJ_F32 (HBM-bound), SPLIT for SJ_F64 (bound by FP64 arithmetic, where SPLIT
+   does the fewest operations) */
+enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1, SJ_SCHED_TMA = 2 };
 
 #define SJ_MAX_POLES 8
 #define SJ_MAX_SOURCES 4
@@ -255,14 +258,16 @@ int sj_set_stream(sj_sim* sim, void* cuda_stream);
 int sj_set_schedule(sj_sim* sim, int32_t schedule);
 int sj_synchronize(sj_sim* sim);
 
-/* fused-schedule tiling: tiles of 32 x tile_y cells, `rows` consecutive rows
-   per thread ((tile_y, rows) in {(4,1), (8,1), (16,1), (8,2), (16,2)}),
-   z segments of zseg planes (each block marches one segment) */
-int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t rows, int32_t zseg);
-int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* rows, int32_t* zseg);
+/* tiling of the single-pass schedules.  FUSED: blocks of 32 x 8 columns
+   march z segments of zseg in {8, 16, 32, 64} planes (tile_y, ring ignored).
+   TMA: tiles of 32 x tile_y cells, a TMA ring of `ring` planes
+   ((tile_y, ring) in {(4,3), (8,3), (16,3), (4,4), (8,4)}), z segments of
+   zseg planes.  Applies to the schedule selected when it is called. */
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg);
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* ring, int32_t* zseg);
 /* time every fused tiling with `steps` launches that leave the state
    untouched, keep the fastest and report it (any output may be NULL) */
-int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* rows, int32_t* zseg,
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* ring, int32_t* zseg,
                 float* ms_per_step);
 
 /* ---------------------------------------------------------------- stepping */
@@ -289,6 +294,9 @@ int sj_transfer_bytes(const sj_sim* sim, int64_t* h2d, int64_t* d2h);
 /* per-instance voxel count and algorithmic bytes per step (roofline model) */
 int64_t sj_voxels(const sj_sim* sim, int32_t inst);
 double sj_bytes_per_step(const sj_sim* sim, int32_t inst);
+/* kernel launches one sj_step step issues under the current schedule (GB300
+   query; the reference has no counterpart) */
+int32_t sj_launches_per_step(const sj_sim* sim);
 
 /* ---------------------------------------------------------------- read-back */
 /* field_times (src/disp.hpp:172): out[monitor][sample], monitor = order of

@@ -20,7 +20,7 @@ SJ_E_TIMEOUT = -6
 EX, EY, EZ, HX, HY, HZ = range(6)
 COMPONENTS = {"Ex": EX, "Ey": EY, "Ez": EZ, "Hx": HX, "Hy": HY, "Hz": HZ}
 F64, F32 = 0, 1
-SCHED_FUSED, SCHED_SPLIT = 0, 1
+SCHED_FUSED, SCHED_SPLIT, SCHED_TMA = 0, 1, 2
 SRC_GAUSSIAN, SRC_CONTINUOUS = 0, 1
 PROBE_MONITOR, PROBE_DFT = 1, 2
 CSG_BOX, CSG_SPHERE, CSG_CYLINDER, CSG_PLANE = 0, 1, 2, 3
@@ -120,6 +120,7 @@ SIGNATURES = {
     "sj_n_samples": (C.c_int64, [_P, C.c_int32]),
     "sj_voxels": (C.c_int64, [_P, C.c_int32]),
     "sj_bytes_per_step": (C.c_double, [_P, C.c_int32]),
+    "sj_launches_per_step": (C.c_int32, [_P]),
     "sj_read_monitors": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_dft": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

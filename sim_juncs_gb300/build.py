@@ -12,10 +12,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsj_gb300.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["sj_host.cu", "sj_step.cu", "sj_fused.cu", "sj_raster.cu"]
+SOURCES = ["sj_host.cu", "sj_step.cu", "sj_lean.cu", "sj_fused.cu", "sj_raster.cu"]
 HEADERS = ["sj_internal.h", "sj_physics.cuh", os.path.join("..", "..", "include", "sj.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# the fused stepper writes every fused multiply-add explicitly (results must
+# not depend on which of its kernels updated a voxel)
+FILE_FLAGS = {"sj_lean.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -44,7 +47,7 @@ def build(verbose=False, force=False, extra_flags=()):
         op = os.path.join(OBJ, src.replace(".cu", ".o"))
         objs.append(op)
         if force or _stale(op, [sp] + hdrs):
-            jobs.append([nvcc, *ARCH, *FLAGS, *extra_flags, "-c", sp, "-o", op])
+            jobs.append([nvcc, *ARCH, *FLAGS, *FILE_FLAGS.get(src, []), *extra_flags, "-c", sp, "-o", op])
 
     def run(cmd):
         if verbose:

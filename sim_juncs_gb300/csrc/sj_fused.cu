@@ -5,25 +5,28 @@
 // component crosses HBM once in and once out per step.
 //
 // Work decomposition: a block owns a 32 x TY column tile of (x, y) and marches
-// along z over one z segment.  For each plane k:
-//   * every per-plane input of plane k+NS-1 is fetched by TMA
-//     (cp.async.bulk.tensor.3d) into an NS-slot shared-memory ring: E^n and
-//     H^{n-1/2} boxes starting at (i0-XOFF, j0-1) so the x/y halos arrive with
-//     them (out-of-range coordinates read as zero = the domain's outside), the
-//     material-combo bytes of the own cells and, where the tile or plane
-//     touches a CPML slab, that axis' psi_H (own + halo) and psi_E (own) tiles;
-//   * main warps (ty < TY) update H of their own cells of plane k from the
-//     ring, store them, and publish them in shared memory; the halo warp
-//     (ty == TY) recomputes H on the x-1 column and y-1 row that E needs,
-//     without storing them (the neighbour tile owns them);
-//   * main warps update E of plane k from the shared H plane and the own-cell
-//     H of plane k-1 kept in registers, with CPML, sources and polarisation.
+// along z over one z segment; warp w < TY owns row j0+w, warp TY is the halo
+// warp.  The march is skewed by one plane: iteration h updates H of plane h
+// and E of plane h-1, which read different (double-buffered) shared rows, so
+// one barrier per plane suffices and the two updates overlap.
+//   * Per-plane inputs arrive by TMA (cp.async.bulk.tensor.3d) in an NS-slot
+//     shared-memory ring: E^n and H^{n-1/2} boxes from (i0-XOFF, j0-1), so the
+//     x/y halos come with them (out-of-range coordinates read as zero, the
+//     domain's outside), the combo bytes and, where the tile or plane touches
+//     a CPML slab, that axis' psi_H tiles.
+//   * H(h): main warps from the ring; the halo warp recomputes H on the y-1
+//     row and x-1 column (owned by neighbour tiles, not stored).  Own Hx/Hz go
+//     to a shared row for the next warp's y-1 neighbour; x-1 neighbours are
+//     exchanged by warp shuffle (lane 0 takes the halo column).
+//   * E(h-1): from the shared rows of plane h-1, own H of planes h-1 and h-2
+//     and E^n and the combo byte of the own cell kept in registers since the
+//     previous iteration; psi_E of the own cell is read from global memory at
+//     the top of the iteration, so the H work hides its latency.
 // A z segment starting at z0 > 0 first recomputes H of plane z0-1 (owned by
-// the previous segment) to seed the k-1 registers.
-// Extra blocks after the stepping blocks sample monitors and accumulate DFTs
-// from buffer `cur`, which no block writes during the launch.
-// Every wait on an mbarrier gives up after one second and records
-// SJ_E_TIMEOUT in the device status instead of spinning forever.
+// the previous segment), unstored.  Extra blocks after the stepping blocks
+// sample monitors and accumulate DFTs from buffer `cur`, which no block writes
+// during the launch.  Every wait on an mbarrier gives up after 100 ms and
+// records SJ_E_TIMEOUT in the device status instead of spinning forever.
 #include <cuda.h>
 
 #include "sj_physics.cuh"
@@ -32,7 +35,9 @@ namespace sj {
 
 constexpr int FTX = 32;
 constexpr int MAXF_FUSED = 256;
-constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s
+constexpr unsigned long long WAIT_NS = 100000000ull;  // 100 ms (a healthy copy takes microseconds)
+constexpr int MAXC_SMEM = 16;       // combos whose coefficient rows are staged in shared memory
+constexpr int NCOEF_MAX = 3 + 3 * MAXP;
 
 // tensor-map slots of one instance
 constexpr int TM_E = 0, TM_H = 6, TM_C = 12, TM_PE = 13, TM_PH = 19, TM_COUNT = 31;
@@ -48,20 +53,13 @@ struct Box<double> {
     static constexpr int BX = 36, XOFF = 2;  // 288-byte rows, x0 = i0 - 2 (16-byte aligned)
 };
 
-constexpr int NSLOT = 3;           // planes in the TMA ring (k, k+1 and one in flight)
-constexpr int MAXC_SMEM = 16;       // combos whose coefficient rows are staged in shared memory
-constexpr int NCOEF_MAX = 3 + 3 * MAXP;
-
-// Tile = 32 x TY cells, TY = W * R: W main warps of R rows each, plus one halo warp.
-template <typename real, int W, int R>
+template <typename real, int TY, int NS>
 struct Lay {
-    static constexpr int TY = W * R;
-    static constexpr int NS = NSLOT;
     static constexpr int BX = Box<real>::BX;
     static constexpr int XOFF = Box<real>::XOFF;
     static constexpr int RS = (int)sizeof(real);
-    // per ring slot: E boxes (TY+2 rows from j0-1), H boxes and psi_H boxes
-    // (TY+1 rows from j0-1), combo and psi_E boxes (own cells, from (i0, j0))
+    // per ring slot: E boxes (TY+2 rows from j0-1), H boxes (TY+1 rows from
+    // j0-1), combo and psi_H boxes (own cells, from (i0, j0))
     static constexpr int EBOXB = (TY + 2) * BX * RS;
     static constexpr int HBOXB = (TY + 1) * BX * RS;
     static constexpr int CBOXB = TY * 32;
@@ -72,16 +70,17 @@ struct Lay {
     static constexpr int OBOXP = (OBOXB + 127) / 128 * 128;
     static constexpr int OFF_H = 3 * EBOXP;
     static constexpr int OFF_C = OFF_H + 3 * HBOXP;
-    static constexpr int OFF_PE = OFF_C + CBOXP;             // 6 psi_E boxes [axis][pair]
-    static constexpr int OFF_PH = OFF_PE + 6 * OBOXP;        // 6 psi_H boxes [axis][pair]
-    static constexpr int SLOT = OFF_PH + 6 * HBOXP;
+    static constexpr int OFF_PH = OFF_C + CBOXP;             // 6 psi_H boxes [axis][pair]
+    static constexpr int SLOT = OFF_PH + 6 * OBOXP;
     static constexpr int TXB = 3 * EBOXB + 3 * HBOXB + CBOXB; // bytes per plane without psi
-    static constexpr int TXPSI = 2 * OBOXB + 2 * HBOXB;       // extra bytes per CPML axis
+    static constexpr int TXPSI = 2 * OBOXB;                   // extra bytes per CPML axis
     static constexpr int RING = NS * SLOT;
-    // shared H exchange: row j0-1+w*R (Hx, Hz) per warp boundary, column i0-1 (Hy, Hz)
-    static constexpr int OFF_ROW = RING;                      // [W][2][32]
-    static constexpr int OFF_COL = OFF_ROW + W * 2 * FTX * RS;  // [2][TY]
-    static constexpr int OFF_PROF = OFF_COL + 2 * TY * RS;    // x [4][33], y [4][TY+1]
+    // shared H exchange, double-buffered by plane parity:
+    // rows [2][TY+1][Hx, Hz][32] (index 0 = the y-1 halo row, w+1 = warp w),
+    // halo column [2][Hy, Hz][TY]
+    static constexpr int OFF_ROW = RING;
+    static constexpr int OFF_COL = OFF_ROW + 2 * (TY + 1) * 2 * FTX * RS;
+    static constexpr int OFF_PROF = OFF_COL + 2 * 2 * TY * RS;  // x [4][33], y [4][TY+1]
     static constexpr int PROF = 4 * (FTX + 1 + TY + 1) * RS;
     static constexpr int OFF_COEF = (OFF_PROF + PROF + 15) / 16 * 16;  // [MAXC_SMEM][NCOEF_MAX]
     static constexpr int OFF_FLAG = OFF_COEF + MAXC_SMEM * NCOEF_MAX * RS;
@@ -198,46 +197,55 @@ __device__ void probe_block(const InstDev<real>& I, long long chunk, long long n
 }
 
 // --------------------------------------------------------------- stepping blocks
-// CPML state of one cell for the current plane: for each axis, whether the
-// cell lies in that axis' slab, and the profile values b, c there.
+// CPML state of one cell for one plane: per axis, slab membership and b, c.
 template <typename real>
 struct Cpml {
     bool on[3];
     real b[3], c[3];
 };
 
-// curl of component CA with its CPML terms, psi_old read from the ring
-// (pin: 6 boxes [axis][pair], `pst` elements apart, at the cell's position)
-// and psi_new written to global memory at offset o.  Same operation order as
-// curl_psi: cur = d1 - d2; += psi(A1); -= psi(A2).
-template <typename real, int CA>
-__device__ __forceinline__ real curl_ring(const Cpml<real>& cp, real d1, real d2, const real* pin,
-                                          int pst, real* const* pout, long long o, long long vol,
-                                          bool store) {
+// psi_old of the 6 [axis][pair] auxiliaries of one cell, either in registers
+// (get(A, P) with compile-time indices) or in the shared ring.
+template <typename real>
+struct PsiRegs {
+    real v[6];
+    __device__ __forceinline__ real get(int a, int p) const { return v[a * 2 + p]; }
+};
+template <typename real>
+struct PsiRing {
+    const real* base;
+    int stride;
+    __device__ __forceinline__ real get(int a, int p) const { return base[(a * 2 + p) * stride]; }
+};
+
+// curl of component CA with its CPML terms; psi_new goes to global memory at
+// offset o.  Same operation order as curl_psi: cur = d1 - d2; += psi(A1); -= psi(A2).
+template <typename real, int CA, typename Psi>
+__device__ __forceinline__ real curl_c(const Cpml<real>& cp, real d1, real d2, const Psi& pin,
+                                       real* const* pout, long long o, long long vol, bool store) {
     constexpr int A1 = (CA + 1) % 3, A2 = (CA + 2) % 3;
     constexpr int P1 = (CA > A1) ? CA - 1 : CA;
     constexpr int P2 = (CA > A2) ? CA - 1 : CA;
     real cur = d1 - d2;
     if (cp.on[A1]) {
-        const real psi = cp.b[A1] * pin[(A1 * 2 + P1) * pst] + cp.c[A1] * d1;
+        const real psi = cp.b[A1] * pin.get(A1, P1) + cp.c[A1] * d1;
         if (store) pout[A1][P1 * vol + o] = psi;
         cur += psi;
     }
     if (cp.on[A2]) {
-        const real psi = cp.b[A2] * pin[(A2 * 2 + P2) * pst] + cp.c[A2] * d2;
+        const real psi = cp.b[A2] * pin.get(A2, P2) + cp.c[A2] * d2;
         if (store) pout[A2][P2 * vol + o] = psi;
         cur -= psi;
     }
     return cur;
 }
 
-template <typename real, int W, int R>
+template <typename real, int TY, int NS>
 __device__ void step_block(const InstDev<real>& I, long long local, long long n, int cur, bool dry,
                            DevState* st, unsigned char* smem) {
-    using L = Lay<real, W, R>;
-    constexpr int TY = L::TY, NS = L::NS;
-    real* sRow = reinterpret_cast<real*>(smem + L::OFF_ROW);    // [W][Hx, Hz][32]
-    real* sCol = reinterpret_cast<real*>(smem + L::OFF_COL);    // [Hy, Hz][TY]
+    using L = Lay<real, TY, NS>;
+    real* sRow = reinterpret_cast<real*>(smem + L::OFF_ROW);   // [2][TY+1][Hx, Hz][32]
+    real* sCol = reinterpret_cast<real*>(smem + L::OFF_COL);   // [2][Hy, Hz][TY]
     real* prof = reinterpret_cast<real*>(smem + L::OFF_PROF);  // [4][33] x, then [4][TY+1] y
     real* scoef = reinterpret_cast<real*>(smem + L::OFF_COEF);
     unsigned char* sflag = smem + L::OFF_FLAG;
@@ -254,7 +262,7 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
     const int z0 = zseg * I.f_zs;
     const int z1 = min(I.nz, z0 + I.f_zs);
     const int kstart = z0 > 0 ? z0 - 1 : 0;
-    const int kend = z1;  // planes kstart..kend are read (k+1 of the last plane z1-1)
+    const int kend = z1;  // H of planes kstart..kend-1 reads planes kstart..kend
 
     // does the tile (incl. its x-1 / y-1 halo) touch the x / y CPML slabs?
     const bool tile_x = (I.pl[0] > 0 && i0 - 1 < I.pl[0]) || (I.ph[0] > 0 && i0 + FTX - 1 >= I.nx - I.ph[0]);
@@ -269,11 +277,11 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     // CPML profiles of the tile's columns (i0-1 .. i0+31) and rows (j0-1 .. j0+TY-1),
-    // and the first MAXC_SMEM rows of the combo table
+    // and the combo table when it is small
     const bool coef_smem = I.n_combos <= MAXC_SMEM;
     {
         const int t = w * FTX + tx;
-        const int nthr = FTX * (W + 1);
+        const int nthr = FTX * (TY + 1);
         for (int q = t; q < 4 * (FTX + 1); q += nthr) {
             const int a = q / (FTX + 1), x = i0 - 1 + q % (FTX + 1);
             prof[q] = (x >= 0 && x < I.nx) ? I.prof[0][a * I.nx + x] : real(0);
@@ -291,10 +299,11 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
     const real* coef = coef_smem ? scoef : I.coef;
     const unsigned char* cflag = coef_smem ? sflag : I.cflag;
 
+    auto in_z = [&](int p) { return have_z && (p < I.pl[2] || p >= I.nz - I.ph[2]); };
     auto issue = [&](int p, int sl) {  // plane p into ring slot sl (lead thread only)
         const uint32_t bar = smem_u32(&bars[sl]);
         unsigned char* base = smem + sl * L::SLOT;
-        const bool pz = have_z && (p < I.pl[2] || p >= I.nz - I.ph[2]);
+        const bool pz = in_z(p);
         const uint32_t bytes = (uint32_t)(L::TXB + L::TXPSI * ((int)tile_x + (int)tile_y + (int)pz));
         mbar_expect_tx(bar, bytes);
         const int xh = i0 - L::XOFF, yh = j0 - 1;
@@ -306,12 +315,9 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
         tma_load_3d(smem_u32(base + L::OFF_C), tm + TM_C * 128, i0, j0, p, bar);
         for (int a = 0; a < 3; ++a) {
             if (!(a == 0 ? tile_x : (a == 1 ? tile_y : pz))) continue;
-            for (int pp = 0; pp < 2; ++pp) {
-                tma_load_3d(smem_u32(base + L::OFF_PE + (a * 2 + pp) * L::OBOXP), tm + (TM_PE + a * 2 + pp) * 128,
-                            i0, j0, p, bar);
-                tma_load_3d(smem_u32(base + L::OFF_PH + (a * 2 + pp) * L::HBOXP),
-                            tm + (TM_PH + cur * 6 + a * 2 + pp) * 128, xh, yh, p, bar);
-            }
+            for (int pp = 0; pp < 2; ++pp)
+                tma_load_3d(smem_u32(base + L::OFF_PH + (a * 2 + pp) * L::OBOXP),
+                            tm + (TM_PH + cur * 6 + a * 2 + pp) * 128, i0, j0, p, bar);
         }
     };
     if (lead)
@@ -319,6 +325,7 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
 
     const real S = I.S;
     const long long vol = I.vol;
+    real* const* psiHin = I.psiH[cur];
     real* const* psiHout = I.psiH[cur ^ 1];
     real* const* psiE = I.psiE;
     real* const Hx = I.F[cur ^ 1][3];
@@ -328,21 +335,23 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
     real* const Ey = I.F[cur ^ 1][1];
     real* const Ez = I.F[cur ^ 1][2];
 
-    const bool main = w < W;
-    const int i = i0 + tx;
-    const int jb = j0 + w * R;          // first row of this warp
-    const bool xin = i < I.nx;
+    const bool main = w < TY;
+    const int i = i0 + tx, j = j0 + w;
+    const bool own = main && i < I.nx && j < I.ny;
     // halo cells of the halo warp: y-1 row (hr) and x-1 column (hc)
     const int hri = i0 + tx, hrj = j0 - 1;
     const int hci = i0 - 1, hcj = j0 + tx;
     const bool hrow = !main && hrj >= 0 && hri < I.nx;
     const bool hcol = !main && tx < TY && hci >= 0 && hcj < I.ny;
-    const int xp = tx + 1;  // own column's index in the shared x profile
-    const bool xon = in_slab(I, 0, i);
+    const int xp = tx + 1, yp = w + 1;  // own cell's index in the shared profiles
+    const bool xon = in_slab(I, 0, i), yon = in_slab(I, 1, j);
     const bool xon_r = in_slab(I, 0, hri), yon_r = in_slab(I, 1, hrj);
     const bool xon_c = in_slab(I, 0, hci), yon_c = in_slab(I, 1, hcj);
     const real* px = prof;                   // [4][FTX+1]
     const real* py = prof + 4 * (FTX + 1);   // [4][TY+1]
+    const long long oij = (long long)j * I.px + i;
+    const long long oij_r = (long long)hrj * I.px + hri;
+    const long long oij_c = (long long)hcj * I.px + hci;
     // sources overlapping this tile's footprint (own cells and halo), one bit per source
     unsigned smask = 0;
     for (int q = 0; q < I.n_src; ++q) {
@@ -351,114 +360,150 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
             sv.lo[1] + sv.n[1] > j0 - 1)
             smask |= 1u << q;
     }
-
-    constexpr int EB = L::EBOXP / L::RS, HBX = L::HBOXP / L::RS, OB = L::OBOXP / L::RS;
-    // shared-memory element offsets inside a ring slot, row r of this warp
-    // E / H / psi_H boxes start at (i0-XOFF, j0-1); combo / psi_E boxes at (i0, j0)
-    const int e_own0 = (w * R + 1) * L::BX + tx + L::XOFF;
-    const int o_own0 = w * R * FTX + tx;
-    const int e_row = tx + L::XOFF;                      // halo row cell (box row 0)
-    const int e_col = (tx + 1) * L::BX + L::XOFF - 1;    // halo column cell
-
-    real hx_prev[R], hy_prev[R];  // H^{n+1/2} of plane k-1 at the own cells
-#pragma unroll
-    for (int r = 0; r < R; ++r) hx_prev[r] = hy_prev[r] = 0;
-    bool ok = true;
-    int s0 = 0, s1 = 1 % NS;        // ring slots of planes k and k+1
-    unsigned par0 = 0, par1 = (1 / NS) & 1;
-
-    for (int k = kstart; k < kend; ++k) {
-        const int q = k - kstart;
-        const bool storing = k >= z0;
-        const bool zon = have_z && (k < I.pl[2] || k >= I.nz - I.ph[2]);
-        real bzi = 0, czi = 0, bzh = 0, czh = 0;
-        if (zon) {
-            bzi = I.prof[2][k];
-            czi = I.prof[2][I.nz + k];
-            bzh = I.prof[2][2 * I.nz + k];
-            czh = I.prof[2][3 * I.nz + k];
-        }
-        unsigned pm = 0;  // sources that touch this plane (block-uniform)
+    auto plane_sources = [&](int p) {
+        unsigned pm = 0;
         for (unsigned m = smask; m; m &= m - 1) {
             const int qq = __ffs(m) - 1;
             const SrcDev<real>& sv = I.src[qq];
-            if (k >= sv.lo[2] && k < sv.lo[2] + sv.n[2]) pm |= 1u << qq;
+            if (p >= sv.lo[2] && p < sv.lo[2] + sv.n[2]) pm |= 1u << qq;
         }
-        // wait for planes k and k+1
-        if (q == 0) ok &= mbar_wait(smem_u32(&bars[s0]), par0);
-        ok &= mbar_wait(smem_u32(&bars[s1]), par1);
-        if (!ok) abort_flag = 1;
+        return pm;
+    };
 
-        const real* E0 = reinterpret_cast<const real*>(smem + s0 * L::SLOT);      // E of plane k
-        const real* E1 = reinterpret_cast<const real*>(smem + s1 * L::SLOT);      // E of plane k+1
-        const real* H0 = reinterpret_cast<const real*>(smem + s0 * L::SLOT + L::OFF_H);
-        const real* PH = reinterpret_cast<const real*>(smem + s0 * L::SLOT + L::OFF_PH);
-        const real* PE = reinterpret_cast<const real*>(smem + s0 * L::SLOT + L::OFF_PE);
-        const unsigned char* CBX = smem + s0 * L::SLOT + L::OFF_C;
-        const long long o_plane = (long long)k * I.plane;
+    constexpr int EB = L::EBOXP / L::RS, HBX = L::HBOXP / L::RS, OB = L::OBOXP / L::RS;
+    // shared-memory element offsets inside a ring slot
+    const int e_own = (w + 1) * L::BX + tx + L::XOFF;    // E / H boxes: own cell
+    const int o_own = w * FTX + tx;                      // combo / psi_H boxes: own cell
+    const int e_row = tx + L::XOFF;                      // halo row cell (box row 0)
+    const int e_col = (tx + 1) * L::BX + L::XOFF - 1;    // halo column cell
 
-        real hx[R], hy[R], hz[R];
-        // ---------------- H phase
+    // registers carried across the skewed march
+    real hx1 = 0, hy1 = 0, hz1 = 0;  // own H of the E plane e = h-1
+    real hx2 = 0, hy2 = 0;           // own H of plane e-1
+    real eo0 = 0, eo1 = 0, eo2 = 0;  // own E^n of plane e
+    int cbe = 0;                     // own combo of plane e
+    // psi registers: main warps keep psi_E of plane e in p0; the halo warp keeps
+    // psi_H of plane h for its row cell in p0 and its column cell in p1
+    PsiRegs<real> p0, p1;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) p0.v[q] = p1.v[q] = 0;
+    bool zon_e = false;
+    real bzi_e = 0, czi_e = 0;
+    unsigned pm_e = 0;
+    bool ok = true;
+    int sa = 0, sb = 1 % NS;         // ring slots of planes h and h+1
+    unsigned pa = 0, pb = (1 / NS) & 1;
+
+    for (int h = kstart; h <= kend; ++h) {
+        const bool do_h = h < kend;
+        const bool store_h = h >= z0;            // H(h) is this segment's to store
+        const bool do_e = h - 1 >= z0;           // E(h-1)
+        const int q = h - kstart;
+        const bool zon = in_z(h);
+        real bzh = 0, czh = 0, bzi = 0, czi = 0;
+        if (zon && do_h) {
+            bzi = I.prof[2][h];
+            czi = I.prof[2][I.nz + h];
+            bzh = I.prof[2][2 * I.nz + h];
+            czh = I.prof[2][3 * I.nz + h];
+        }
+        const unsigned pm = do_h ? plane_sources(h) : 0u;
+        // global psi reads of this iteration, issued first so the H work hides them
         if (main) {
-            const bool st_psi = storing && !dry;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int j = jb + r;
-                hx[r] = hy[r] = hz[r] = 0;
-                if (!(xin && j < I.ny)) continue;
-                const long long o = o_plane + (long long)j * I.px + i;
-                const int eo = e_own0 + r * L::BX;
-                const real* e = E0 + eo;
-                const real ex = e[0], ey = e[EB], ez = e[2 * EB];
-                const real ex_j = e[L::BX], ey_i = e[EB + 1], ez_i = e[2 * EB + 1], ez_j = e[2 * EB + L::BX];
-                const real ex_k = E1[eo], ey_k = E1[EB + eo];
-                Cpml<real> cp;
-                cp.on[0] = xon;
-                cp.on[1] = in_slab(I, 1, j);
-                cp.on[2] = zon;
-                cp.b[0] = px[2 * (FTX + 1) + xp];
-                cp.c[0] = px[3 * (FTX + 1) + xp];
-                cp.b[1] = py[2 * (TY + 1) + w * R + r + 1];
-                cp.c[1] = py[3 * (TY + 1) + w * R + r + 1];
-                cp.b[2] = bzh;
-                cp.c[2] = czh;
-                const real* pin = PH + eo;
-                {
-                    const real cv = curl_ring<real, 0>(cp, ez_j - ez, ey_k - ey, pin, HBX, psiHout, o, vol, st_psi);
-                    real acc = -(S * cv);
-                    if (pm) acc = apply_sources(I, SJ_HX, i, j, k, n, acc);
-                    hx[r] = H0[eo] + acc;
-                }
-                {
-                    const real cv = curl_ring<real, 1>(cp, ex_k - ex, ez_i - ez, pin, HBX, psiHout, o, vol, st_psi);
-                    real acc = -(S * cv);
-                    if (pm) acc = apply_sources(I, SJ_HY, i, j, k, n, acc);
-                    hy[r] = H0[HBX + eo] + acc;
-                }
-                if (storing) {
-                    const real cv = curl_ring<real, 2>(cp, ey_i - ey, ex_j - ex, pin, HBX, psiHout, o, vol, st_psi);
-                    real acc = -(S * cv);
-                    if (pm) acc = apply_sources(I, SJ_HZ, i, j, k, n, acc);
-                    hz[r] = H0[2 * HBX + eo] + acc;
-                    Hx[o] = hx[r];
-                    Hy[o] = hy[r];
-                    Hz[o] = hz[r];
-                }
+            if (do_e && own) {  // psi_E of the E plane (updated in place by its owner, us)
+                const long long o = (long long)(h - 1) * I.plane + oij;
+                if (xon) { p0.v[0] = psiE[0][o]; p0.v[1] = psiE[0][vol + o]; }
+                if (yon) { p0.v[2] = psiE[1][o]; p0.v[3] = psiE[1][vol + o]; }
+                if (zon_e) { p0.v[4] = psiE[2][o]; p0.v[5] = psiE[2][vol + o]; }
             }
-            if (!storing) {
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    hx_prev[r] = hx[r];
-                    hy_prev[r] = hy[r];
-                }
-            } else if (w + 1 < W) {
-                // this warp's last row is the next warp's y-1 neighbour
-                sRow[(w + 1) * 2 * FTX + tx] = hx[R - 1];
-                sRow[((w + 1) * 2 + 1) * FTX + tx] = hz[R - 1];
+        } else if (do_h && store_h) {  // halo psi_H (read-only: the neighbour tile owns it)
+            const long long op = (long long)h * I.plane;
+            if (hrow) {
+                const long long o = op + oij_r;
+                if (xon_r) p0.v[1] = psiHin[0][vol + o];
+                if (yon_r) { p0.v[2] = psiHin[1][o]; p0.v[3] = psiHin[1][vol + o]; }
+                if (zon) p0.v[4] = psiHin[2][o];
             }
-        } else if (storing) {
-            // halo warp: y-1 row (Hx, Hz) ...
+            if (hcol) {
+                const long long o = op + oij_c;
+                if (xon_c) { p1.v[0] = psiHin[0][o]; p1.v[1] = psiHin[0][vol + o]; }
+                if (yon_c) p1.v[3] = psiHin[1][vol + o];
+                if (zon) p1.v[5] = psiHin[2][vol + o];
+            }
+        }
+        if (do_h) {
+            if (q == 0) ok &= mbar_wait(smem_u32(&bars[sa]), pa);
+            ok &= mbar_wait(smem_u32(&bars[sb]), pb);
+            if (!ok) abort_flag = 1;
+        }
+        const real* E0 = reinterpret_cast<const real*>(smem + sa * L::SLOT);      // E of plane h
+        const real* E1 = reinterpret_cast<const real*>(smem + sb * L::SLOT);      // E of plane h+1
+        const real* H0 = reinterpret_cast<const real*>(smem + sa * L::SLOT + L::OFF_H);
+        const real* PH = reinterpret_cast<const real*>(smem + sa * L::SLOT + L::OFF_PH);
+        const unsigned char* CBX = smem + sa * L::SLOT + L::OFF_C;
+        const long long o_plane = (long long)h * I.plane;
+        real* rowb = sRow + (h & 1) * (TY + 1) * 2 * FTX;     // rows of plane h
+        real* colb = sCol + (h & 1) * 2 * TY;
+        const real* rowe = sRow + ((h - 1) & 1) * (TY + 1) * 2 * FTX;  // rows of plane h-1
+        const real* cole = sCol + ((h - 1) & 1) * 2 * TY;
+
+        // ---------------- H(h)
+        real hx0 = 0, hy0 = 0, hz0 = 0;
+        real eon0 = 0, eon1 = 0, eon2 = 0;
+        int cbn = 0;
+        if (do_h && own) {
+            const long long o = o_plane + oij;
+            const real* e = E0 + e_own;
+            const real ex = e[0], ey = e[EB], ez = e[2 * EB];
+            const real ex_j = e[L::BX], ey_i = e[EB + 1], ez_i = e[2 * EB + 1], ez_j = e[2 * EB + L::BX];
+            const real ex_k = E1[e_own], ey_k = E1[EB + e_own];
+            const bool st_psi = store_h && !dry;
+            Cpml<real> cp;
+            cp.on[0] = xon;
+            cp.on[1] = yon;
+            cp.on[2] = zon;
+            cp.b[0] = px[2 * (FTX + 1) + xp];
+            cp.c[0] = px[3 * (FTX + 1) + xp];
+            cp.b[1] = py[2 * (TY + 1) + yp];
+            cp.c[1] = py[3 * (TY + 1) + yp];
+            cp.b[2] = bzh;
+            cp.c[2] = czh;
+            const PsiRing<real> pin{PH + o_own, OB};
             {
+                const real cv = curl_c<real, 0>(cp, ez_j - ez, ey_k - ey, pin, psiHout, o, vol, st_psi);
+                real acc = -(S * cv);
+                if (pm) acc = apply_sources(I, SJ_HX, i, j, h, n, acc);
+                hx0 = H0[e_own] + acc;
+            }
+            {
+                const real cv = curl_c<real, 1>(cp, ex_k - ex, ez_i - ez, pin, psiHout, o, vol, st_psi);
+                real acc = -(S * cv);
+                if (pm) acc = apply_sources(I, SJ_HY, i, j, h, n, acc);
+                hy0 = H0[HBX + e_own] + acc;
+            }
+            {
+                const real cv = curl_c<real, 2>(cp, ey_i - ey, ex_j - ex, pin, psiHout, o, vol, st_psi);
+                real acc = -(S * cv);
+                if (pm) acc = apply_sources(I, SJ_HZ, i, j, h, n, acc);
+                hz0 = H0[2 * HBX + e_own] + acc;
+            }
+            if (store_h) {
+                Hx[o] = hx0;
+                Hy[o] = hy0;
+                Hz[o] = hz0;
+                // inputs of E(h), used next iteration: E^n and the combo byte
+                eon0 = ex;
+                eon1 = ey;
+                eon2 = ez;
+                cbn = CBX[o_own];
+            }
+        }
+        if (do_h && store_h) {
+            if (main) {
+                rowb[(w + 1) * 2 * FTX + tx] = hx0;
+                rowb[((w + 1) * 2 + 1) * FTX + tx] = hz0;
+            } else {
+                // halo warp: y-1 row (Hx, Hz) ...
                 real vx = 0, vz = 0;
                 if (hrow) {
                     const real* e = E0 + e_row;
@@ -473,129 +518,129 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
                     cp.c[1] = py[3 * (TY + 1)];
                     cp.b[2] = bzh;
                     cp.c[2] = czh;
-                    const real* pin = PH + e_row;
-                    const long long o = o_plane + (long long)hrj * I.px + hri;
+                    const long long o = o_plane + oij_r;
                     {
-                        const real cv = curl_ring<real, 0>(cp, e[2 * EB + L::BX] - ez, E1[EB + e_row] - ey, pin, HBX,
-                                                           psiHout, o, vol, false);
+                        const real cv = curl_c<real, 0>(cp, e[2 * EB + L::BX] - ez, E1[EB + e_row] - ey, p0,
+                                                        psiHout, o, vol, false);
                         real acc = -(S * cv);
-                        if (pm) acc = apply_sources(I, SJ_HX, hri, hrj, k, n, acc);
+                        if (pm) acc = apply_sources(I, SJ_HX, hri, hrj, h, n, acc);
                         vx = H0[e_row] + acc;
                     }
                     {
-                        const real cv = curl_ring<real, 2>(cp, e[EB + 1] - ey, e[L::BX] - ex, pin, HBX, psiHout, o,
-                                                           vol, false);
+                        const real cv = curl_c<real, 2>(cp, e[EB + 1] - ey, e[L::BX] - ex, p0, psiHout, o,
+                                                        vol, false);
                         real acc = -(S * cv);
-                        if (pm) acc = apply_sources(I, SJ_HZ, hri, hrj, k, n, acc);
+                        if (pm) acc = apply_sources(I, SJ_HZ, hri, hrj, h, n, acc);
                         vz = H0[2 * HBX + e_row] + acc;
                     }
                 }
-                sRow[tx] = vx;
-                sRow[FTX + tx] = vz;
-            }
-            // ... and x-1 column (Hy, Hz)
-            if (tx < TY) {
-                real vy = 0, vz = 0;
-                if (hcol) {
-                    const real* e = E0 + e_col;
-                    const real ex = e[0], ey = e[EB], ez = e[2 * EB];
-                    Cpml<real> cp;
-                    cp.on[0] = xon_c;
-                    cp.on[1] = yon_c;
-                    cp.on[2] = zon;
-                    cp.b[0] = px[2 * (FTX + 1)];
-                    cp.c[0] = px[3 * (FTX + 1)];
-                    cp.b[1] = py[2 * (TY + 1) + tx + 1];
-                    cp.c[1] = py[3 * (TY + 1) + tx + 1];
-                    cp.b[2] = bzh;
-                    cp.c[2] = czh;
-                    const real* pin = PH + e_col;
-                    const long long o = o_plane + (long long)hcj * I.px + hci;
-                    {
-                        const real cv = curl_ring<real, 1>(cp, E1[e_col] - ex, e[2 * EB + 1] - ez, pin, HBX, psiHout,
-                                                           o, vol, false);
-                        real acc = -(S * cv);
-                        if (pm) acc = apply_sources(I, SJ_HY, hci, hcj, k, n, acc);
-                        vy = H0[HBX + e_col] + acc;
+                rowb[tx] = vx;
+                rowb[FTX + tx] = vz;
+                // ... and x-1 column (Hy, Hz)
+                if (tx < TY) {
+                    real vy = 0, vz2 = 0;
+                    if (hcol) {
+                        const real* e = E0 + e_col;
+                        const real ex = e[0], ey = e[EB], ez = e[2 * EB];
+                        Cpml<real> cp;
+                        cp.on[0] = xon_c;
+                        cp.on[1] = yon_c;
+                        cp.on[2] = zon;
+                        cp.b[0] = px[2 * (FTX + 1)];
+                        cp.c[0] = px[3 * (FTX + 1)];
+                        cp.b[1] = py[2 * (TY + 1) + tx + 1];
+                        cp.c[1] = py[3 * (TY + 1) + tx + 1];
+                        cp.b[2] = bzh;
+                        cp.c[2] = czh;
+                        const long long o = o_plane + oij_c;
+                        {
+                            const real cv = curl_c<real, 1>(cp, E1[e_col] - ex, e[2 * EB + 1] - ez, p1, psiHout,
+                                                            o, vol, false);
+                            real acc = -(S * cv);
+                            if (pm) acc = apply_sources(I, SJ_HY, hci, hcj, h, n, acc);
+                            vy = H0[HBX + e_col] + acc;
+                        }
+                        {
+                            const real cv = curl_c<real, 2>(cp, e[EB + 1] - ey, e[L::BX] - ex, p1, psiHout, o,
+                                                            vol, false);
+                            real acc = -(S * cv);
+                            if (pm) acc = apply_sources(I, SJ_HZ, hci, hcj, h, n, acc);
+                            vz2 = H0[2 * HBX + e_col] + acc;
+                        }
                     }
-                    {
-                        const real cv = curl_ring<real, 2>(cp, e[EB + 1] - ey, e[L::BX] - ex, pin, HBX, psiHout, o,
-                                                           vol, false);
-                        real acc = -(S * cv);
-                        if (pm) acc = apply_sources(I, SJ_HZ, hci, hcj, k, n, acc);
-                        vz = H0[2 * HBX + e_col] + acc;
-                    }
+                    colb[tx] = vy;
+                    colb[TY + tx] = vz2;
                 }
-                sCol[tx] = vy;
-                sCol[TY + tx] = vz;
             }
         }
-        __syncthreads();
-
-        // ---------------- E phase
-        if (main && storing) {
-            const bool st_in = !dry;
-            const bool src_e = pm != 0;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int j = jb + r;
-                // x-1 neighbours by shuffle (lane 0 takes the halo column)
-                real hy_i = __shfl_up_sync(0xffffffffu, hy[r], 1);
-                real hz_i = __shfl_up_sync(0xffffffffu, hz[r], 1);
-                if (tx == 0) {
-                    hy_i = sCol[w * R + r];
-                    hz_i = sCol[TY + w * R + r];
-                }
-                // y-1 neighbours from the row above (this thread, or the shared row)
-                const real hx_j = r > 0 ? hx[r > 0 ? r - 1 : 0] : sRow[w * 2 * FTX + tx];
-                const real hz_j = r > 0 ? hz[r > 0 ? r - 1 : 0] : sRow[(w * 2 + 1) * FTX + tx];
-                if (!(xin && j < I.ny)) continue;
-                const long long o = o_plane + (long long)j * I.px + i;
-                const int eo = e_own0 + r * L::BX;
-                const int oo = o_own0 + r * FTX;
-                const int cb = CBX[oo];
-                const real* cf = coef + cb * I.ncoef;
-                const bool disp = (cflag[cb] & 1) != 0;
+        // ---------------- E(h-1): shared rows/column of plane h-1 are complete
+        // since the barrier that ended the previous iteration
+        if (do_e && main) {
+            const int e = h - 1;
+            // x-1 neighbours by shuffle (lane 0 takes the halo column)
+            real hy_i = __shfl_up_sync(0xffffffffu, hy1, 1);
+            real hz_i = __shfl_up_sync(0xffffffffu, hz1, 1);
+            if (tx == 0) {
+                hy_i = cole[w];
+                hz_i = cole[TY + w];
+            }
+            // y-1 neighbours from the row above (the halo row for warp 0)
+            const real hx_j = rowe[w * 2 * FTX + tx];
+            const real hz_j = rowe[(w * 2 + 1) * FTX + tx];
+            if (own) {
+                const long long o = (long long)e * I.plane + oij;
+                const real* cf = coef + cbe * I.ncoef;
+                const bool disp = (cflag[cbe] & 1) != 0;
+                const bool st_in = !dry;
+                const bool src_e = pm_e != 0;
                 Cpml<real> cp;
                 cp.on[0] = xon;
-                cp.on[1] = in_slab(I, 1, j);
-                cp.on[2] = zon;
+                cp.on[1] = yon;
+                cp.on[2] = zon_e;
                 cp.b[0] = px[xp];
                 cp.c[0] = px[(FTX + 1) + xp];
-                cp.b[1] = py[w * R + r + 1];
-                cp.c[1] = py[(TY + 1) + w * R + r + 1];
-                cp.b[2] = bzi;
-                cp.c[2] = czi;
-                const real* pin = PE + oo;
-                const real* e = E0 + eo;
+                cp.b[1] = py[yp];
+                cp.c[1] = py[(TY + 1) + yp];
+                cp.b[2] = bzi_e;
+                cp.c[2] = czi_e;
                 {
-                    const real cv = curl_ring<real, 0>(cp, hz[r] - hz_j, hy[r] - hy_prev[r], pin, OB, psiE, o, vol, st_in);
-                    Ex[o] = e_finish_row<real, 0>(I, i, j, k, n, cf, disp, e[0], cv, st_in, src_e);
+                    const real cv = curl_c<real, 0>(cp, hz1 - hz_j, hy1 - hy2, p0, psiE, o, vol, st_in);
+                    Ex[o] = e_finish_row<real, 0>(I, i, j, e, n, cf, disp, eo0, cv, st_in, src_e);
                 }
                 {
-                    const real cv = curl_ring<real, 1>(cp, hx[r] - hx_prev[r], hz[r] - hz_i, pin, OB, psiE, o, vol, st_in);
-                    Ey[o] = e_finish_row<real, 1>(I, i, j, k, n, cf, disp, e[EB], cv, st_in, src_e);
+                    const real cv = curl_c<real, 1>(cp, hx1 - hx2, hz1 - hz_i, p0, psiE, o, vol, st_in);
+                    Ey[o] = e_finish_row<real, 1>(I, i, j, e, n, cf, disp, eo1, cv, st_in, src_e);
                 }
                 {
-                    const real cv = curl_ring<real, 2>(cp, hy[r] - hy_i, hx[r] - hx_j, pin, OB, psiE, o, vol, st_in);
-                    Ez[o] = e_finish_row<real, 2>(I, i, j, k, n, cf, disp, e[2 * EB], cv, st_in, src_e);
+                    const real cv = curl_c<real, 2>(cp, hy1 - hy_i, hx1 - hx_j, p0, psiE, o, vol, st_in);
+                    Ez[o] = e_finish_row<real, 2>(I, i, j, e, n, cf, disp, eo2, cv, st_in, src_e);
                 }
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                hx_prev[r] = hx[r];
-                hy_prev[r] = hy[r];
             }
         }
+        // shift the carried registers: plane h becomes the E plane
+        hx2 = hx1;
+        hy2 = hy1;
+        hx1 = hx0;
+        hy1 = hy0;
+        hz1 = hz0;
+        eo0 = eon0;
+        eo1 = eon1;
+        eo2 = eon2;
+        cbe = cbn;
+        zon_e = zon;
+        bzi_e = bzi;
+        czi_e = czi;
+        pm_e = pm;
         __syncthreads();
         if (abort_flag) break;
-        // slot s0 is free: fetch plane k + NS into it
-        if (lead && k + NS <= kend) issue(k + NS, s0);
-        // advance the ring: plane k+1 is now in s0, plane k+2 in the next slot
-        s0 = s1;
-        par0 = par1;
-        if (++s1 == NS) s1 = 0;
-        par1 = (unsigned)(((q + 2) / NS) & 1);
+        if (do_h) {
+            // slot sa (plane h) is free: fetch plane h + NS into it
+            if (lead && h + NS <= kend) issue(h + NS, sa);
+            sa = sb;
+            pa = pb;
+            if (++sb == NS) sb = 0;
+            pb = (unsigned)(((q + 2) / NS) & 1);
+        }
     }
     if (abort_flag) {
         if (lead) {
@@ -607,8 +652,15 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
     }
 }
 
-template <typename real, int W, int R>
-__global__ void __launch_bounds__(FTX * (W + 1))
+// Blocks per SM the register budget aims for.  FP64 steps are bound by the
+// FP64 pipe rather than by latency, so they trade occupancy for no spills.
+template <typename real, int TY>
+struct MinBlocks {
+    static constexpr int value = sizeof(real) == 8 ? (TY <= 4 ? 2 : 1) : (TY <= 4 ? 4 : (TY <= 8 ? 2 : 1));
+};
+
+template <typename real, int TY, int NS>
+__global__ void __launch_bounds__(FTX * (TY + 1), MinBlocks<real, TY>::value)
 k_fused(const InstDev<real>* __restrict__ insts, int n_inst, DevState* st, FusedLaunch fl) {
     extern __shared__ __align__(128) unsigned char smem[];
     // the instance descriptor lives in shared memory for the whole block, so
@@ -630,7 +682,7 @@ k_fused(const InstDev<real>* __restrict__ insts, int n_inst, DevState* st, Fused
     }
     __syncthreads();
     if (stepping)
-        step_block<real, W, R>(sI, lb - pre[ii], n, cur, fl.dry != 0, st, smem);
+        step_block<real, TY, NS>(sI, lb - pre[ii], n, cur, fl.dry != 0, st, smem);
     else if (!fl.dry)
         probe_block<real>(sI, lb - pre[ii], n, cur, st, reinterpret_cast<double2*>(smem));
     // the last block to finish advances the step and flips the buffers
@@ -649,31 +701,31 @@ k_fused(const InstDev<real>* __restrict__ insts, int n_inst, DevState* st, Fused
     }
 }
 
-template <typename real, int W, int R>
-static cudaError_t launch_wr(const InstDev<real>* d, int n_inst, DevState* st, const FusedLaunch& fl,
-                             cudaStream_t s) {
-    using L = Lay<real, W, R>;
+template <typename real, int TY, int NS>
+static cudaError_t launch_t(const InstDev<real>* d, int n_inst, DevState* st, const FusedLaunch& fl,
+                            cudaStream_t s) {
+    using L = Lay<real, TY, NS>;
     const int bytes = L::BYTES > 2 * MAXF_FUSED * 16 ? L::BYTES : 2 * MAXF_FUSED * 16;
     if (bytes > FUSED_MAX_SMEM) return cudaErrorInvalidConfiguration;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_fused<real, W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaError_t e = cudaFuncSetAttribute(k_fused<real, TY, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     const long long blocks = fl.n_items + fl.n_probe_blocks;
-    k_fused<real, W, R><<<(unsigned)blocks, dim3(FTX, W + 1), bytes, s>>>(d, n_inst, st, fl);
+    k_fused<real, TY, NS><<<(unsigned)blocks, dim3(FTX, TY + 1), bytes, s>>>(d, n_inst, st, fl);
     return cudaGetLastError();
 }
 
-// Supported tilings: (tile rows, rows per thread) -> W = tile_y / rows main warps.
-#define SJ_FUSED_TILINGS(X) X(4, 1) X(8, 1) X(16, 1) X(8, 2) X(16, 2)
+// Supported tilings: (tile rows, TMA ring depth).
+#define SJ_FUSED_TILINGS(X) X(4, 3) X(8, 3) X(16, 3) X(4, 4) X(8, 4)
 
 template <typename real>
 cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState* st,
                               const FusedLaunch& fl, cudaStream_t s) {
-#define SJ_CASE(TYV, RV) \
-    if (fl.ty == TYV && fl.rows == RV) return launch_wr<real, TYV / RV, RV>(d_insts, n_inst, st, fl, s);
+#define SJ_CASE(TYV, NV) \
+    if (fl.ty == TYV && fl.ring == NV) return launch_t<real, TYV, NV>(d_insts, n_inst, st, fl, s);
     SJ_FUSED_TILINGS(SJ_CASE)
 #undef SJ_CASE
     return cudaErrorInvalidValue;
@@ -687,19 +739,19 @@ template <>
 int fused_box_xoff<float>() { return Box<float>::XOFF; }
 template <>
 int fused_box_xoff<double>() { return Box<double>::XOFF; }
-int fused_block_threads(int ty, int rows) { return FTX * (ty / rows + 1); }
+int fused_block_threads(int ty) { return FTX * (ty + 1); }
+int fused_tensor_maps() { return TM_COUNT; }
 
 template <typename real>
-int fused_smem_bytes(int ty, int rows) {
-#define SJ_CASE(TYV, RV) \
-    if (ty == TYV && rows == RV) return Lay<real, TYV / RV, RV>::BYTES;
+int fused_smem_bytes(int ty, int ring) {
+#define SJ_CASE(TYV, NV) \
+    if (ty == TYV && ring == NV) return Lay<real, TYV, NV>::BYTES;
     SJ_FUSED_TILINGS(SJ_CASE)
 #undef SJ_CASE
     return -1;
 }
 template int fused_smem_bytes<float>(int, int);
 template int fused_smem_bytes<double>(int, int);
-int fused_tensor_maps() { return TM_COUNT; }
 
 template cudaError_t launch_fused_step<double>(const InstDev<double>*, int, DevState*, const FusedLaunch&,
                                                cudaStream_t);

@@ -139,15 +139,29 @@ struct sj_sim {
     cudaGraphExec_t graph = nullptr;
     int graph_chunk = 0;
     int graph_sched = -1;
-    // fused schedule: tiling, tensor maps, block prefixes
-    int f_ty = 8, f_zs = 64, f_rows = 1;
+    // TMA schedule: tiling, tensor maps, block prefixes
+    int f_ty = 8, f_zs = 64, f_ring = 3;
     bool fused_ready = false;
     FusedLaunch fl{};
     void* d_fpre = nullptr;
     void* d_tmaps = nullptr;
+    // fused (lean) schedule: z-segment length (descriptors travel as kernel
+    // parameters) and the side streams its kernels overlap on
+    int l_zb = 16;
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    // bumped whenever a descriptor changes; a graph holding parameter copies
+    // of older descriptors is captured again
+    long long table_version = 0;
+    long long graph_version = -1;
 
     ~sj_sim() {
         if (stream) cudaStreamSynchronize(stream);
+        for (int q = 0; q < 2; ++q) {
+            if (side[q]) cudaStreamSynchronize(side[q]), cudaStreamDestroy(side[q]);
+            if (ev_join[q]) cudaEventDestroy(ev_join[q]);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -611,6 +625,7 @@ void upload_table(sj_sim* sim) {
     ck(cudaStreamSynchronize(sim->stream), "sync before table upload");
     ck(cudaMemcpy(sim->d_table, buf.data(), buf.size(), cudaMemcpyHostToDevice), "table upload");
     sim->h2d += (long long)buf.size();
+    sim->table_version += 1;
 }
 
 // Make sure source tables and monitor buffers cover steps [0, t_end).
@@ -686,7 +701,7 @@ void prepare_fused(sj_sim* sim) {
     const int nmaps = fused_tensor_maps();
     std::vector<CUtensorMap> maps((size_t)n * nmaps);
     std::vector<long long> pre(2 * (n + 1), 0);
-    const int thr = fused_block_threads(ty, sim->f_rows);
+    const int thr = fused_block_threads(ty);
     for (int q = 0; q < n; ++q) {
         InstDev<real>& I = dv[q];
         const cuuint64_t dims[3] = {(cuuint64_t)I.nx, (cuuint64_t)I.ny, (cuuint64_t)I.nz};
@@ -704,7 +719,7 @@ void prepare_fused(sj_sim* sim) {
             sizeof(real) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         const cuuint32_t bx = (cuuint32_t)fused_box_width<real>();
         // slots: [0..5] E[b][c] (halo box), [6..11] H[b][c] (halo box), [12] combo (own box),
-        // [13..18] psi_E[a][pair] (own box), [19..30] psi_H[b][a][pair] (halo box)
+        // [13..18] psi_E[a][pair] (own box), [19..30] psi_H[b][a][pair] (own box)
         CUtensorMap* m = &maps[(size_t)q * nmaps];
         for (int b = 0; b < 2; ++b)
             for (int c = 0; c < 3; ++c) {
@@ -719,7 +734,7 @@ void prepare_fused(sj_sim* sim) {
                 enc(m + 13 + a * 2 + pp, fdt, pe, sizeof(real), 32, (cuuint32_t)ty);
                 for (int b = 0; b < 2; ++b) {
                     real* ph = I.psiH[b][a] ? I.psiH[b][a] + (size_t)pp * I.vol : I.F[0][3];
-                    enc(m + 19 + b * 6 + a * 2 + pp, fdt, ph, sizeof(real), bx, (cuuint32_t)(ty + 1));
+                    enc(m + 19 + b * 6 + a * 2 + pp, fdt, ph, sizeof(real), 32, (cuuint32_t)ty);
                 }
             }
         I.f_ntx = (I.nx + 31) / 32;
@@ -736,7 +751,7 @@ void prepare_fused(sj_sim* sim) {
     for (int q = 0; q < n; ++q) dv[q].tmap = reinterpret_cast<const CUtensorMap*>(sim->d_tmaps) + (size_t)q * nmaps;
     FusedLaunch& fl = sim->fl;
     fl.ty = ty;
-    fl.rows = sim->f_rows;
+    fl.ring = sim->f_ring;
     fl.n_items = pre[n];
     fl.n_probe_blocks = pre[2 * n + 1];
     fl.d_item_pre = reinterpret_cast<const long long*>(sim->d_fpre);
@@ -747,10 +762,29 @@ void prepare_fused(sj_sim* sim) {
 }
 
 template <typename real>
+void prepare_schedule(sj_sim* sim) {
+    if (sim->schedule == SJ_SCHED_TMA) prepare_fused<real>(sim);
+}
+
+// Side streams and events of the fused schedule, created on first use.
+LeanStreams lean_streams(sj_sim* sim) {
+    if (!sim->ev_fork) {
+        for (int q = 0; q < 2; ++q) {
+            ck(cudaStreamCreateWithFlags(&sim->side[q], cudaStreamNonBlocking), "side stream");
+            ck(cudaEventCreateWithFlags(&sim->ev_join[q], cudaEventDisableTiming), "event");
+        }
+        ck(cudaEventCreateWithFlags(&sim->ev_fork, cudaEventDisableTiming), "event");
+    }
+    return LeanStreams{sim->stream, {sim->side[0], sim->side[1]}, sim->ev_fork, {sim->ev_join[0], sim->ev_join[1]}};
+}
+
+template <typename real>
 cudaError_t launch_one(sj_sim* sim) {
     auto& dv = devv<real>(sim);
     const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
-    if (sim->schedule == SJ_SCHED_FUSED) {
+    if (sim->schedule == SJ_SCHED_FUSED)
+        return launch_lean_step<real>(dv.data(), sim->n_inst, sim->l_zb, 0, sim->d_state, lean_streams(sim));
+    if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         return launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
     }
@@ -759,26 +793,65 @@ cudaError_t launch_one(sj_sim* sim) {
 
 // Time `steps` dry launches (no state change) of every tiling candidate and
 // keep the fastest: the project's own autotuner for the fused schedule.
+// Lean-schedule autotuner: z-segment length by timing dry launches.
 template <typename real>
-void autotune(sj_sim* sim, int steps, int* best_ty, int* best_rows, int* best_zs, float* best_ms) {
+void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
+    const int zbs[4] = {8, 16, 32, 64};
+    float best = 1e30f;
+    int bzb = sim->l_zb;
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    ensure_capacity<real>(sim, sim->t + 1);
+    const auto& dv = devv<real>(sim);
+    const LeanStreams ls = lean_streams(sim);
+    for (int zb : zbs) {
+        ck(launch_lean_step<real>(dv.data(), sim->n_inst, zb, 1, sim->d_state, ls), "autotune");
+        ck(cudaEventRecord(e0, sim->stream), "event");
+        for (int q = 0; q < steps; ++q)
+            ck(launch_lean_step<real>(dv.data(), sim->n_inst, zb, 1, sim->d_state, ls), "autotune");
+        ck(cudaEventRecord(e1, sim->stream), "event");
+        ck(cudaEventSynchronize(e1), "event");
+        float ms = 0;
+        ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+        if (ms < best) {
+            best = ms;
+            bzb = zb;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sim->l_zb = bzb;
+    if (best_zs) *best_zs = bzb;
+    if (best_ms) *best_ms = best / steps;
+}
+
+template <typename real>
+void autotune(sj_sim* sim, int steps, int* best_ty, int* best_ring, int* best_zs, float* best_ms) {
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        autotune_lean<real>(sim, steps, best_zs, best_ms);
+        if (best_ty) *best_ty = 8;
+        if (best_ring) *best_ring = 0;
+        return;
+    }
     int nzmax = 1;
     for (auto& I : devv<real>(sim)) nzmax = std::max(nzmax, I.nz);
-    const int tilings[5][2] = {{4, 1}, {8, 1}, {16, 1}, {8, 2}, {16, 2}};
+    const int tilings[5][2] = {{4, 3}, {8, 3}, {16, 3}, {4, 4}, {8, 4}};
     const int zss[3] = {32, 64, nzmax};
     float best = 1e30f;
-    int bty = sim->f_ty, bzs = sim->f_zs, brows = sim->f_rows;
+    int bty = sim->f_ty, bzs = sim->f_zs, bring = sim->f_ring;
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     ensure_capacity<real>(sim, sim->t + 1);
     for (const auto& tl : tilings)
         for (int zs : zss) {
-            const int ty = tl[0], rows = tl[1];
-            const int sb = fused_smem_bytes<real>(ty, rows);
+            const int ty = tl[0], ring = tl[1];
+            const int sb = fused_smem_bytes<real>(ty, ring);
             if (sb < 0 || sb > FUSED_MAX_SMEM) continue;  // does not fit one SM
             sim->f_ty = ty;
             sim->f_zs = zs;
-            sim->f_rows = rows;
+            sim->f_ring = ring;
             sim->fused_ready = false;
             prepare_fused<real>(sim);
             FusedLaunch fl = sim->fl;
@@ -796,19 +869,19 @@ void autotune(sj_sim* sim, int steps, int* best_ty, int* best_rows, int* best_zs
                 best = ms;
                 bty = ty;
                 bzs = zs;
-                brows = rows;
+                bring = ring;
             }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     sim->f_ty = bty;
     sim->f_zs = bzs;
-    sim->f_rows = brows;
+    sim->f_ring = bring;
     sim->fused_ready = false;
     prepare_fused<real>(sim);
     if (best_ty) *best_ty = bty;
     if (best_zs) *best_zs = bzs;
-    if (best_rows) *best_rows = brows;
+    if (best_ring) *best_ring = bring;
     if (best_ms) *best_ms = best / steps;
 }
 
@@ -817,7 +890,7 @@ void do_steps(sj_sim* sim, long long n) {
     ensure_capacity<real>(sim, sim->t + n);
     for (long long q = 0; q < n; ++q) ck(launch_one<real>(sim), "step launch");
     sim->t += n;
-    if (sim->schedule == SJ_SCHED_FUSED && (n & 1)) sim->cur ^= 1;
+    if (sim->schedule != SJ_SCHED_SPLIT && (n & 1)) sim->cur ^= 1;
 }
 
 template <typename real>
@@ -825,8 +898,9 @@ void do_steps_graph(sj_sim* sim, long long n, int chunk) {
     if (chunk < 1) fail(SJ_E_INVALID, "chunk must be >= 1");
     ensure_capacity<real>(sim, sim->t + n);
     // everything that allocates or copies happens before the capture
-    if (sim->schedule == SJ_SCHED_FUSED) prepare_fused<real>(sim);
-    if (!sim->graph || sim->graph_chunk != chunk || sim->graph_sched != sim->schedule) {
+    prepare_schedule<real>(sim);
+    if (!sim->graph || sim->graph_chunk != chunk || sim->graph_sched != sim->schedule ||
+        sim->graph_version != sim->table_version) {
         if (sim->graph) cudaGraphExecDestroy(sim->graph);
         sim->graph = nullptr;
         cudaStream_t cs;
@@ -853,6 +927,7 @@ void do_steps_graph(sj_sim* sim, long long n, int chunk) {
         ck(e, "graph instantiate");
         sim->graph_chunk = chunk;
         sim->graph_sched = sim->schedule;
+        sim->graph_version = sim->table_version;
     }
     long long left = n;
     while (left >= chunk) {
@@ -861,7 +936,7 @@ void do_steps_graph(sj_sim* sim, long long n, int chunk) {
     }
     for (long long q = 0; q < left; ++q) ck(launch_one<real>(sim), "step launch");
     sim->t += n;
-    if (sim->schedule == SJ_SCHED_FUSED && (n & 1)) sim->cur ^= 1;
+    if (sim->schedule != SJ_SCHED_SPLIT && (n & 1)) sim->cur ^= 1;
 }
 
 int finish(sj_sim* sim, int code, const std::string& msg) {
@@ -1013,21 +1088,31 @@ int sj_set_stream(sj_sim* sim, void* stream) {
 
 int sj_set_schedule(sj_sim* sim, int32_t schedule) {
     if (!sim) return SJ_E_INVALID;
-    if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT)
+    if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT && schedule != SJ_SCHED_TMA)
         return finish(sim, SJ_E_INVALID, "unknown schedule");
     sim->schedule = schedule;
     return SJ_OK;
 }
 
-int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t rows, int32_t zseg) {
+int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {
     if (!sim) return SJ_E_INVALID;
-    const int sb = sim->precision == SJ_F64 ? fused_smem_bytes<double>(tile_y, rows)
-                                            : fused_smem_bytes<float>(tile_y, rows);
-    if (sb < 0) return finish(sim, SJ_E_INVALID, "unsupported tiling (tile_y, rows)");
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        if (zseg != 8 && zseg != 16 && zseg != 32 && zseg != 64)
+            return finish(sim, SJ_E_INVALID, "fused schedule: zseg must be 8, 16, 32 or 64");
+        sim->l_zb = zseg;
+        if (sim->graph) {
+            cudaGraphExecDestroy(sim->graph);
+            sim->graph = nullptr;
+        }
+        return SJ_OK;
+    }
+    const int sb = sim->precision == SJ_F64 ? fused_smem_bytes<double>(tile_y, ring)
+                                            : fused_smem_bytes<float>(tile_y, ring);
+    if (sb < 0) return finish(sim, SJ_E_INVALID, "unsupported tiling (tile_y, ring)");
     if (sb > FUSED_MAX_SMEM) return finish(sim, SJ_E_INVALID, "tiling needs more shared memory than one SM has");
     if (zseg < 1) return finish(sim, SJ_E_INVALID, "zseg must be >= 1");
     sim->f_ty = tile_y;
-    sim->f_rows = rows;
+    sim->f_ring = ring;
     sim->f_zs = zseg;
     sim->fused_ready = false;
     if (sim->graph) {
@@ -1037,15 +1122,21 @@ int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t rows, int32_t zseg) {
     return SJ_OK;
 }
 
-int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* rows, int32_t* zseg) {
-    if (!sim || !tile_y || !rows || !zseg) return SJ_E_INVALID;
+int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* ring, int32_t* zseg) {
+    if (!sim || !tile_y || !ring || !zseg) return SJ_E_INVALID;
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        *tile_y = 8;
+        *ring = 0;
+        *zseg = sim->l_zb;
+        return SJ_OK;
+    }
     *tile_y = sim->f_ty;
-    *rows = sim->f_rows;
+    *ring = sim->f_ring;
     *zseg = sim->f_zs;
     return SJ_OK;
 }
 
-int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* rows, int32_t* zseg,
+int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* ring, int32_t* zseg,
                 float* ms_per_step) {
     if (!sim || steps < 1) return SJ_E_INVALID;
     SJ_TRY(sim)
@@ -1054,9 +1145,9 @@ int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* rows, int3
         sim->graph = nullptr;
     }
     if (sim->precision == SJ_F64)
-        autotune<double>(sim, steps, tile_y, rows, zseg, ms_per_step);
+        autotune<double>(sim, steps, tile_y, ring, zseg, ms_per_step);
     else
-        autotune<float>(sim, steps, tile_y, rows, zseg, ms_per_step);
+        autotune<float>(sim, steps, tile_y, ring, zseg, ms_per_step);
     check_status(sim);
     SJ_CATCH(sim)
 }
@@ -1112,6 +1203,17 @@ double sj_time(const sj_sim* sim, int32_t inst) {
 double sj_last_source_time(const sj_sim* sim, int32_t inst) { INST_GET(last_source_time, NAN) }
 int64_t sj_voxels(const sj_sim* sim, int32_t inst) { INST_GET(voxels, -1) }
 double sj_bytes_per_step(const sj_sim* sim, int32_t inst) { INST_GET(bytes_per_step, NAN) }
+int32_t sj_launches_per_step(const sj_sim* sim) {
+    if (!sim) return -1;
+    if (sim->schedule == SJ_SCHED_FUSED)
+        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), sim->n_inst, sim->l_zb)
+                                        : lean_launches(sim->h32.data(), sim->n_inst, sim->l_zb);
+    if (sim->schedule == SJ_SCHED_TMA) return 1;
+    int maxp = 0;
+    for (int q = 0; q < sim->n_inst; ++q)
+        maxp = std::max(maxp, sim->precision == SJ_F64 ? sim->h64[q].n_probe : sim->h32[q].n_probe);
+    return maxp > 0 ? 3 : 2;  // probe, H pass, E pass
+}
 int64_t sj_n_samples(const sj_sim* sim, int32_t inst) {
     if (!sim || inst < 0 || inst >= sim->n_inst) return -1;
     const int ss = sim->precision == SJ_F64 ? sim->hi64[inst].save_span : sim->hi32[inst].save_span;

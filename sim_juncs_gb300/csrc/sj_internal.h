@@ -96,8 +96,8 @@ cudaError_t launch_split_step(const InstDev<real>* d_insts, const InstDev<real>*
                               int n_inst, DevState* st, cudaStream_t s);
 // Fused schedule launch description (host side).
 struct FusedLaunch {
-    int ty;                     // tile height (4, 8 or 16 rows)
-    int rows;                   // rows per thread (2 or 4)
+    int ty;                     // TMA schedule: tile height; lean schedule: z-segment length
+    int ring;                   // TMA ring depth (planes)
     long long n_items;          // stepping blocks (tiles x z segments)
     long long n_probe_blocks;   // probe blocks after them
     const long long* d_item_pre;   // [n_inst + 1] prefix of stepping blocks
@@ -107,14 +107,46 @@ struct FusedLaunch {
 template <typename real>
 cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState* st,
                               const FusedLaunch& fl, cudaStream_t s);
+// Fused (lean) schedule: each launch carries its instance descriptors as a
+// kernel parameter; a step is a general-, a single-slab- and a plain-tile
+// launch per group of at most LEAN_TAB instances, and the last block of all
+// of them advances the step counter.
+constexpr int LEAN_TAB = 32;
+template <typename real, int K>
+struct LeanTable {
+    int n_inst;                 // descriptors used, <= K
+    int dry;                    // 1 = time only: no step advance, no in-place stores
+    unsigned step_blocks;       // blocks of all launches of the step
+    int any_slab;               // some instance has CPML slabs
+    long long n_items;          // tiles (one block each); probe blocks follow them in k_lean_general
+    long long item_pre[K + 1];  // prefix of tiles per instance (all tiles)
+    long long plain_pre[K + 1]; // prefix of plain-box tiles per instance
+    long long probe_pre[K + 1]; // prefix of probe blocks per instance
+    int box[K][6];              // plain box in tile coordinates: x0, x1, y0, y1, z0, z1
+    InstDev<real> inst[K];
+};
+long long lean_items(int nx, int ny, int nz, int zb);  // stepping blocks of one instance
+template <typename real>
+int lean_launches(const InstDev<real>* h_insts, int n_inst, int zb);  // launches per step
+// Streams of one fused step: the general kernel runs on `main`, the
+// single-slab and plain kernels on the side streams, forked from and joined
+// back into `main` with the events (side streams null: all on `main`).
+struct LeanStreams {
+    cudaStream_t main;
+    cudaStream_t side[2];
+    cudaEvent_t fork, join[2];
+};
+template <typename real>
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, int n_inst, int zb, int dry, DevState* st,
+                             const LeanStreams& ls);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>
 int fused_box_xoff();           // box starts at i0 - xoff
-int fused_block_threads(int ty, int rows);  // threads per block (= probes per probe block)
+int fused_block_threads(int ty);  // threads per block (= probes per probe block)
 int fused_tensor_maps();          // CUtensorMap slots per instance
 template <typename real>
-int fused_smem_bytes(int ty, int rows);  // dynamic shared memory of a tiling, -1 if unsupported
+int fused_smem_bytes(int ty, int ring);  // dynamic shared memory of a tiling, -1 if unsupported
 constexpr int FUSED_MAX_SMEM = 227 * 1024;
 template <typename real>
 cudaError_t launch_max_abs_e(const InstDev<real>& h_inst, int buf, double* d_out, cudaStream_t s);

@@ -13,8 +13,9 @@ from . import _abi
 from .spec import Instance
 
 _PREC = {"f64": _abi.F64, "f32": _abi.F32, _abi.F64: _abi.F64, _abi.F32: _abi.F32}
-_SCHED = {"fused": _abi.SCHED_FUSED, "split": _abi.SCHED_SPLIT,
-          _abi.SCHED_FUSED: _abi.SCHED_FUSED, _abi.SCHED_SPLIT: _abi.SCHED_SPLIT}
+_SCHED = {"fused": _abi.SCHED_FUSED, "split": _abi.SCHED_SPLIT, "tma": _abi.SCHED_TMA,
+          _abi.SCHED_FUSED: _abi.SCHED_FUSED, _abi.SCHED_SPLIT: _abi.SCHED_SPLIT,
+          _abi.SCHED_TMA: _abi.SCHED_TMA}
 
 
 class Fields:
@@ -71,9 +72,10 @@ class Fields:
     def set_schedule(self, schedule):
         self._ck(self.lib.sj_set_schedule(self.handle, _SCHED[schedule]))
 
-    def set_tiling(self, tile_y, rows, zseg):
-        """Fused-schedule tiling: 32 x tile_y tiles, `rows` rows per thread, z segments."""
-        self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(rows), int(zseg)))
+    def set_tiling(self, tile_y, ring, zseg):
+        """Tiling of the selected single-pass schedule (fused: only zseg; tma:
+        32 x tile_y tiles, TMA ring depth, z segments)."""
+        self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(ring), int(zseg)))
 
     def tiling(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
@@ -82,7 +84,7 @@ class Fields:
 
     def autotune(self, steps=3):
         """Pick the fused tiling by timing state-preserving launches.
-        Returns (tile_y, rows, zseg, ms_per_step)."""
+        Returns (tile_y, ring, zseg, ms_per_step)."""
         a, b, c, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
         self._ck(self.lib.sj_autotune(self.handle, int(steps), C.byref(a), C.byref(b), C.byref(c),
                                       C.byref(ms)))
@@ -132,6 +134,10 @@ class Fields:
         if inst is None:
             return sum(self.lib.sj_bytes_per_step(self.handle, q) for q in range(self.n_instances))
         return self.lib.sj_bytes_per_step(self.handle, inst)
+
+    def launches_per_step(self):
+        """Kernel launches one step issues under the current schedule."""
+        return int(self.lib.sj_launches_per_step(self.handle))
 
     def n_samples(self, inst=0):
         return self.lib.sj_n_samples(self.handle, inst)

@@ -6,6 +6,8 @@ the PML carries the absolute rounding of its peak); FP64 monitor series and
 DFT sums within 1e-10 relative to their own maximum; FP32 gap monitors and
 DFTs within 1e-4 of FP64 (the target for the FP32 path).
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -138,15 +140,15 @@ def test_fused_and_split_agree(lib, precision, tol):
     assert rel(b.monitors(), a.monitors()) <= tol
 
 
-@pytest.mark.parametrize("ty,rows,zs", [(4, 1, 7), (16, 2, 13), (8, 2, 1000), (16, 1, 45)])
-def test_fused_tilings_agree(lib, ty, rows, zs):
+@pytest.mark.parametrize("ty,ring,zs", [(4, 3, 7), (16, 3, 13), (8, 4, 1000), (4, 4, 45)])
+def test_tma_tilings_agree(lib, ty, ring, zs):
     # tile heights, z-segment lengths (incl. ragged ones) and ring depths
     # change only the work decomposition, never the numbers
     inst = junction_instance(n=45, res=14.0)
-    a = Fields(inst, "f32", "fused")
-    b = Fields(inst, "f32", "fused")
-    a.set_tiling(8, 1, 64)
-    b.set_tiling(ty, rows, zs)
+    a = Fields(inst, "f32", "tma")
+    b = Fields(inst, "f32", "tma")
+    a.set_tiling(8, 3, 64)
+    b.set_tiling(ty, ring, zs)
     a.step(60)
     b.step(60)
     for c in range(6):
@@ -154,14 +156,63 @@ def test_fused_tilings_agree(lib, ty, rows, zs):
     np.testing.assert_array_equal(b.monitors(), a.monitors())
 
 
-def test_autotune_leaves_state_untouched(lib):
-    inst = junction_instance(n=40, res=12.5)
+@pytest.mark.parametrize("zs", [8, 32, 64])
+def test_fused_zsegments_agree(lib, zs):
+    # the z-segment length moves tiles between the plain and the general
+    # kernel; both evaluate the same formula, so the bits do not change
+    inst = junction_instance(n=96, res=30.0)
+    assert plain_tiles(inst, 16) > 0          # zs = 64 leaves none: all general
     a = Fields(inst, "f32", "fused")
     b = Fields(inst, "f32", "fused")
+    a.set_tiling(8, 0, 16)
+    b.set_tiling(8, 0, zs)
+    assert b.tiling() == (8, 0, zs)
+    a.step(60)
+    b.step(60)
+    for c in range(6):
+        np.testing.assert_array_equal(b.get_array(c), a.get_array(c))
+    np.testing.assert_array_equal(b.monitors(), a.monitors())
+
+
+def plain_tiles(inst, zb):
+    """A lower bound on the tiles the fused schedule gives its plain kernel
+    (32 x 8 x zb tiles whose footprint, one cell wider towards -x/-y/-z,
+    avoids every CPML slab; slabs taken one cell wider than they are)."""
+    g = inst.grid
+    w = math.ceil(inst.pml.thickness / g.dx) + 1 if inst.pml.thickness > 0 else 0
+
+    def clear(n, t):
+        nt = -(-n // t)
+        return sum(1 for q in range(nt) if max(q * t - 1, 0) >= w and min(q * t + t, n) - 1 < n - w)
+
+    return clear(g.nx, 32) * clear(g.ny, 8) * clear(g.nz, zb)
+
+
+@pytest.mark.parametrize("pml_um", [0.2, 0.0])
+def test_fused_plain_tiles_match_oracle(lib, oracle_lib, pml_um):
+    inst = junction_instance(n=80, res=25.0, pml_um=pml_um)
+    assert plain_tiles(inst, 16) > 0
+    f = Fields(inst, "f64", "fused")
+    o = OracleFields(inst)
+    f.step(250)
+    o.step(250)
+    compare_fields(f, o, TOL64)
+    assert rel(f.monitors(), o.monitors()) <= TOL64
+    assert rel(f.dft(), o.dft()) <= TOL64
+
+
+@pytest.mark.parametrize("schedule", ["fused", "tma"])
+def test_autotune_leaves_state_untouched(lib, schedule):
+    inst = junction_instance(n=40, res=12.5)
+    a = Fields(inst, "f32", schedule)
+    b = Fields(inst, "f32", schedule)
     a.step(50)
     b.step(50)
-    ty, rows, zs, ms = b.autotune(steps=2)
-    assert ty in (4, 8, 16) and rows in (1, 2) and zs >= 1 and ms > 0
+    ty, ring, zs, ms = b.autotune(steps=2)
+    if schedule == "fused":
+        assert (ty, ring) == (8, 0) and zs in (8, 16, 32, 64) and ms > 0
+    else:
+        assert ty in (4, 8, 16) and ring in (3, 4) and zs >= 1 and ms > 0
     assert b.steps_done == 50
     a.step(50)
     b.step(50)
