@@ -9,7 +9,11 @@ whose state is well above L2 (512 x 512 x 384), its roofline fraction, and
 the FP32/FP64 gap-field error.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload sweep|bowtie|junction] [--schedule fused|split]
+                  [--workload sweep|bowtie|junction] [--schedule auto|fused|tma|split]
+
+--schedule auto (default) autotunes both single-pass schedules (fused
+column-march kernels; TMA shared-memory tiles) on the workload and times
+the faster.
 
 Under torchrun each rank runs its own full batch (weak scaling, no
 collective on the data path); value = all ranks' voxel-steps / max time.
@@ -40,7 +44,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="sweep", choices=["sweep", "bowtie", "junction"])
-    p.add_argument("--schedule", default="fused", choices=["fused", "split"])
+    p.add_argument("--schedule", default="auto", choices=["auto", "fused", "tma", "split"])
     p.add_argument("--e2e-steps", type=int, default=400)
     p.add_argument("--no-extras", action="store_true", help="skip the FP64 and error legs")
     return p.parse_args()
@@ -123,7 +127,7 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def time_steps(f, torch, steps, warmup, launches_per_step):
+def time_steps(f, torch, steps, warmup):
     """Device time of `steps` steps on f's stream (CUDA events), after warmup."""
     f.step(warmup)
     f.synchronize()
@@ -138,14 +142,35 @@ def time_steps(f, torch, steps, warmup, launches_per_step):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    return ms / 1000.0, steps * launches_per_step
+    return ms / 1000.0, steps * f.launches_per_step()
+
+
+def tuned_fields(insts, schedule, torch):
+    """Fields on the current torch stream with the schedule's tiling picked by
+    the library's autotuner; schedule "auto" keeps the faster of the two
+    single-pass schedules.  Returns (fields, schedule, tiling, ms/step)."""
+    from sim_juncs_gb300.fields import Fields
+    cands = ("fused", "tma") if schedule == "auto" else (schedule,)
+    best = None
+    for sch in cands:
+        f = Fields(insts, "f32", sch, stream=torch.cuda.current_stream())
+        if sch == "split":
+            til, ms = None, None
+        else:
+            ty, ring, zs, ms = f.autotune(steps=2)
+            til = (ty, ring, zs)
+        if best is None or (ms is not None and ms < best[3]):
+            if best is not None:
+                best[0].close()
+            best = (f, sch, til, ms)
+        else:
+            f.close()
+    return best
 
 
 def run_ours(args):
     import torch
     from sim_juncs_gb300 import build
-    from sim_juncs_gb300.fields import Fields
-    from sim_juncs_gb300 import configs
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -159,18 +184,16 @@ def run_ours(args):
         torch.distributed.barrier()
 
     insts, cfg = workload_instances(args.workload, rank)
-    f = Fields(insts, "f32", args.schedule, stream=torch.cuda.current_stream())
-    if args.schedule == "fused":
-        ty, ring, zs, _ = f.autotune(steps=2)
-        cfg = dict(cfg, tile=f"32x{ty}", tma_ring=ring, zseg=zs, tiling="autotuned")
-    has_probes = any(i.probes for i in insts)
-    lps = (1 if args.schedule == "fused" else 2) + (1 if has_probes and args.schedule == "split" else 0)
+    f, schedule, til, tune_ms = tuned_fields(insts, args.schedule, torch)
+    if til is not None:
+        cfg = dict(cfg, tile=f"32x{til[0]}", tma_ring=til[1], zseg=til[2], tiling="autotuned",
+                   autotune_ms_per_step=tune_ms)
     voxels = f.voxels()
     bytes_step = f.bytes_per_step()
 
     clocks = ClockSampler(local)
     clocks.start()
-    secs, launches = time_steps(f, torch, args.steps, args.warmup, lps)
+    secs, launches = time_steps(f, torch, args.steps, args.warmup)
     clk = clocks.stop()
     t = torch.tensor([secs], device="cuda")
     if ws > 1:
@@ -179,16 +202,18 @@ def run_ours(args):
     value = voxels * args.steps * ws / secs
     peak, peak_kind = measured_peak()
     achieved = bytes_step / (secs / args.steps) / 1e9
+    kernel = {"fused": "fused step: general, single-slab and plain column-march kernels, concurrent",
+              "tma": "k_fused (TMA shared-memory tiles), one launch per step",
+              "split": "k_split_h + k_split_e"}[schedule]
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(cfg, schedule=args.schedule, l2="state larger than L2 (no flush needed)",
+        "config": dict(cfg, schedule=schedule, l2="state larger than L2 (no flush needed)",
                        voxels_per_step=voxels, parallelism=f"replicas{ws}"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": bytes_step,
-                     "kernel": "fused stepper" if args.schedule == "fused" else "split H+E stepper"},
+                     "frac": achieved / peak, "traffic": traffic_per_step(schedule, voxels),
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": bytes_step, "kernel": kernel},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -197,61 +222,81 @@ def run_ours(args):
 
     if rank == 0 and not args.no_extras:
         out["fp64_plain"] = fp64_leg(torch, args)
-        out["fp32_vs_fp64"] = error_leg(args)
+        out["fp32_vs_fp64"] = error_leg(schedule)
     if rank == 0:
-        out["e2e"] = e2e_leg(torch, args, insts)
-        out["cpu_baseline"] = cpu_baseline(args)
+        out["e2e"] = e2e_leg(args, insts, schedule, til)
+        out["cpu_baseline"] = cpu_baseline()
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
 
 
+def traffic_per_step(schedule, voxels):
+    """DRAM bytes per step from the committed ncu summary of the schedule's
+    kernels (bytes per voxel-step of the captured case x this step's voxels),
+    or None when there is none."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            per = json.load(fh)[schedule]["dram_bytes_per_voxel_step"]
+        return float(per) * voxels
+    except Exception:
+        return None
+
+
 def fp64_leg(torch, args):
-    """Plain FP64 path on the 512 x 512 x 384 bowtie grid (state >> L2)."""
+    """Plain FP64 path (the library's FP64 default schedule) on the
+    512 x 512 x 384 bowtie grid (state >> L2)."""
     from sim_juncs_gb300 import configs
     from sim_juncs_gb300.fields import Fields
     inst = configs.bowtie_instance()
-    f = Fields(inst, "f64", args.schedule, stream=torch.cuda.current_stream())
-    if args.schedule == "fused":
-        f.autotune(steps=2)
+    f = Fields(inst, "f64", stream=torch.cuda.current_stream())
     steps = max(5, args.steps // 4)
-    secs, _ = time_steps(f, torch, steps, 3, 1)
+    secs, launches = time_steps(f, torch, steps, 3)
     peak, kind = measured_peak()
     b = f.bytes_per_step()
     ach = b / (secs / steps) / 1e9
-    res = {"workload": "bowtie 512x512x384 f64", "value": inst.grid.voxels * steps / secs, "unit": UNIT,
-           "ms_per_step": secs / steps * 1e3, "steps": steps,
+    res = {"workload": "bowtie 512x512x384 f64", "schedule": f.schedule_name(),
+           "value": inst.grid.voxels * steps / secs, "unit": UNIT,
+           "ms_per_step": secs / steps * 1e3, "steps": steps, "gpu_launches": launches,
            "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "peak_kind": kind, "algorithmic_bytes_per_step": b}}
     f.close()
     return res
 
 
-def error_leg(args):
-    """FP32 vs FP64 relative gap-field error on the 64^3 junction (2000 steps)."""
+def error_leg(schedule):
+    """FP32 (timed schedule) vs FP64 (default schedule) relative gap-field
+    error on the 64^3 junction, 2000 steps."""
     from sim_juncs_gb300 import configs
     from sim_juncs_gb300.fields import Fields
     inst = configs.junction_instance()
-    a = Fields(inst, "f64", args.schedule)
-    b = Fields(inst, "f32", args.schedule)
+    a = Fields(inst, "f64")
+    b = Fields(inst, "f32", schedule)
     a.step(2000)
     b.step(2000)
     m64, m32 = a.monitors()[:4], b.monitors()[:4]
     d64, d32 = a.dft()[:4], b.dft()[:4]
+    a.close()
+    b.close()
     return {"workload": "junction 64^3, 2000 steps, Ex at 4 gap points",
             "monitor_rel_err": float(np.max(np.abs(m32 - m64)) / np.max(np.abs(m64))),
             "dft_rel_err": float(np.max(np.abs(d32 - d64)) / np.max(np.abs(d64)))}
 
 
-def e2e_leg(torch, args, insts):
-    """Whole job through the C ABI from host descriptors: create (uploads the
-    scene, rasterises on the device), e2e_steps steps (source tables go H2D),
-    then monitors + DFT back to host buffers.  Wall clock, host to host."""
+def e2e_leg(args, insts, schedule, til):
+    """Whole job through the public API from host descriptors: create
+    (uploads the scene and the per-step source tables, rasterises on the
+    device), set the tuned tiling, e2e_steps steps, then monitors + DFT back
+    to host buffers.  Wall clock, host to host."""
     from sim_juncs_gb300.fields import Fields
+    import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    f = Fields(insts, "f32", args.schedule)
+    f = Fields(insts, "f32", schedule)
+    if til is not None:
+        f.set_tiling(*til)
     f.step(args.e2e_steps)
     outs = [(f.monitors(q), f.dft(q)) for q in range(f.n_instances)]
     t1 = time.perf_counter()
@@ -270,18 +315,22 @@ def cpu_sample():
     return configs.junction_instance(n=96, res=30.0, probe_components=("Ez",), dft=False)
 
 
-def cpu_baseline(args, steps=60):
+def cpu_baseline(target_s=10.0):
+    """The oracle on one 96^3 sweep member, as many steps as take ~target_s."""
     from oracle import oracle
     oracle.build()
     inst = cpu_sample()
     o = oracle.OracleFields(inst)
-    o.step(2)
+    t0 = time.perf_counter()
+    o.step(10)
+    probe = time.perf_counter() - t0
+    steps = int(min(4000, max(10, target_s / max(probe / 10, 1e-6))))
     t0 = time.perf_counter()
     o.step(steps)
     secs = time.perf_counter() - t0
-    return {"value": inst.grid.voxels * steps / secs, "unit": UNIT, "cores": os.cpu_count(),
-            "kind": "port", "sample": f"one 96^3 sweep member, {steps} FP64 steps (OpenMP restatement; "
-                                       "meep v1.24 is not available to run)"}
+    return {"value": inst.grid.voxels * steps / secs, "unit": UNIT, "cores": oracle.threads(),
+            "kind": "port", "sample": f"one 96^3 sweep member, {steps} FP64 steps in {secs:.1f} s "
+                                       "(OpenMP restatement; meep v1.24 is not available to run)"}
 
 
 def run_reference(args):
@@ -305,7 +354,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference", "config": cfg,
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
                             "sample": f"{per} FP64 steps of one 96^3 sweep member per bench step "
                                       "(CPU restatement; meep v1.24 is not available to run)"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -256,6 +256,8 @@ int sj_destroy(sj_sim* sim);
 /* stream used by every later call (a cudaStream_t); NULL = the library's own */
 int sj_set_stream(sj_sim* sim, void* cuda_stream);
 int sj_set_schedule(sj_sim* sim, int32_t schedule);
+/* the schedule in use (SJ_SCHED_*), -1 for a null handle */
+int32_t sj_get_schedule(const sj_sim* sim);
 int sj_synchronize(sj_sim* sim);
 
 /* tiling of the single-pass schedules.  FUSED: blocks of 32 x 8 columns

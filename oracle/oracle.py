@@ -30,6 +30,11 @@ def build(force=False):
     return LIB
 
 
+def threads():
+    """OpenMP threads the oracle's stepping loops use."""
+    return int(load().sjo_threads())
+
+
 def load():
     global _lib
     if _lib is not None:
@@ -40,6 +45,7 @@ def load():
     P = C.c_void_p
     D = C.POINTER(C.c_double)
     lib.sjo_last_error.restype = C.c_char_p
+    lib.sjo_threads.restype = C.c_int
     lib.sjo_create.argtypes = [C.POINTER(_abi.InstanceDesc), C.POINTER(P)]
     lib.sjo_destroy.argtypes = [P]
     lib.sjo_step.argtypes = [P, C.c_int64]

@@ -34,6 +34,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <omp.h>
 
 namespace {
 
@@ -490,6 +491,8 @@ void step_once(sjo_sim* s) {
 extern "C" {
 
 const char* sjo_last_error(void) { return g_err.c_str(); }
+// OpenMP threads the stepping loops use
+int sjo_threads(void) { return omp_get_max_threads(); }
 
 int sjo_create(const sj_instance_desc* d, sjo_sim** out) {
     *out = nullptr;

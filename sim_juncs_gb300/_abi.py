@@ -121,6 +121,7 @@ SIGNATURES = {
     "sj_voxels": (C.c_int64, [_P, C.c_int32]),
     "sj_bytes_per_step": (C.c_double, [_P, C.c_int32]),
     "sj_launches_per_step": (C.c_int32, [_P]),
+    "sj_get_schedule": (C.c_int32, [_P]),
     "sj_read_monitors": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_dft": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

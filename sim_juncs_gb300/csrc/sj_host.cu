@@ -1086,6 +1086,8 @@ int sj_set_stream(sj_sim* sim, void* stream) {
     SJ_CATCH(sim)
 }
 
+int32_t sj_get_schedule(const sj_sim* sim) { return sim ? sim->schedule : -1; }
+
 int sj_set_schedule(sj_sim* sim, int32_t schedule) {
     if (!sim) return SJ_E_INVALID;
     if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT && schedule != SJ_SCHED_TMA)

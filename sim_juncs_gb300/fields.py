@@ -135,6 +135,11 @@ class Fields:
             return sum(self.lib.sj_bytes_per_step(self.handle, q) for q in range(self.n_instances))
         return self.lib.sj_bytes_per_step(self.handle, inst)
 
+    def schedule_name(self):
+        """The schedule in use: "fused", "split" or "tma"."""
+        return {_abi.SCHED_FUSED: "fused", _abi.SCHED_SPLIT: "split", _abi.SCHED_TMA: "tma"}[
+            int(self.lib.sj_get_schedule(self.handle))]
+
     def launches_per_step(self):
         """Kernel launches one step issues under the current schedule."""
         return int(self.lib.sj_launches_per_step(self.handle))
