@@ -135,8 +135,8 @@ struct sj_sim {
     int cur = 0;                       // host mirror of the ping-pong buffer
     std::vector<void*> allocs;
     std::string err;
-    // graph cache
-    cudaGraphExec_t graph = nullptr;
+    // graph cache, by the parity the captured chunk starts at
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_chunk = 0;
     int graph_sched = -1;
     // TMA schedule: tiling, tensor maps, block prefixes
@@ -148,8 +148,11 @@ struct sj_sim {
     // fused (lean) schedule: z-segment length (descriptors travel as kernel
     // parameters) and the side streams its kernels overlap on
     int l_zb = 16;
-    cudaStream_t side[2] = {nullptr, nullptr};
-    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    int lean_zb = -1;                  // z-segment length the tile lists were built for
+    void* d_tiles = nullptr;           // tile lists of all instances and classes
+    std::vector<LeanTiles> ltiles;     // per instance
+    cudaStream_t side[LEAN_STREAMS] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[LEAN_STREAMS] = {};
     // bumped whenever a descriptor changes; a graph holding parameter copies
     // of older descriptors is captured again
     long long table_version = 0;
@@ -157,14 +160,18 @@ struct sj_sim {
 
     ~sj_sim() {
         if (stream) cudaStreamSynchronize(stream);
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < LEAN_STREAMS; ++q) {
             if (side[q]) cudaStreamSynchronize(side[q]), cudaStreamDestroy(side[q]);
             if (ev_join[q]) cudaEventDestroy(ev_join[q]);
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
-        if (graph) cudaGraphExecDestroy(graph);
+        drop_graphs();
         for (void* p : allocs) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+    void drop_graphs() {
+        for (int p = 0; p < 2; ++p)
+            if (graph[p]) cudaGraphExecDestroy(graph[p]), graph[p] = nullptr;
     }
     void* dalloc(size_t bytes, bool zero = true) {
         void* p = nullptr;
@@ -761,34 +768,75 @@ void prepare_fused(sj_sim* sim) {
     sim->fused_ready = true;
 }
 
+// Tile lists of the fused schedule for the current z-segment length: every
+// instance's tiles by class, in one device buffer.
+template <typename real>
+void prepare_lean(sj_sim* sim) {
+    if (sim->lean_zb == sim->l_zb && sim->d_tiles) return;
+    auto& dv = devv<real>(sim);
+    std::vector<unsigned> all;
+    std::vector<long long> off((size_t)sim->n_inst * LEAN_CLASSES);
+    std::vector<unsigned> lists[LEAN_CLASSES];
+    sim->ltiles.assign(sim->n_inst, LeanTiles{});
+    for (int q = 0; q < sim->n_inst; ++q) {
+        if (lean_classify<real>(dv[q], sim->l_zb, lists) != 0)
+            fail(SJ_E_INVALID, "grid too large for the fused schedule's tile codes");
+        for (int c = 0; c < LEAN_CLASSES; ++c) {
+            off[(size_t)q * LEAN_CLASSES + c] = (long long)all.size();
+            sim->ltiles[q].count[c] = (long long)lists[c].size();
+            all.insert(all.end(), lists[c].begin(), lists[c].end());
+        }
+    }
+    sim->dfree(sim->d_tiles);
+    sim->d_tiles = sim->upload(all);
+    const unsigned* base = reinterpret_cast<const unsigned*>(sim->d_tiles);
+    for (int q = 0; q < sim->n_inst; ++q)
+        for (int c = 0; c < LEAN_CLASSES; ++c)
+            sim->ltiles[q].list[c] = base + off[(size_t)q * LEAN_CLASSES + c];
+    sim->lean_zb = sim->l_zb;
+}
+
 template <typename real>
 void prepare_schedule(sj_sim* sim) {
     if (sim->schedule == SJ_SCHED_TMA) prepare_fused<real>(sim);
+    if (sim->schedule == SJ_SCHED_FUSED) prepare_lean<real>(sim);
 }
 
 // Side streams and events of the fused schedule, created on first use.
 LeanStreams lean_streams(sj_sim* sim) {
     if (!sim->ev_fork) {
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < LEAN_STREAMS; ++q) {
             ck(cudaStreamCreateWithFlags(&sim->side[q], cudaStreamNonBlocking), "side stream");
             ck(cudaEventCreateWithFlags(&sim->ev_join[q], cudaEventDisableTiming), "event");
         }
         ck(cudaEventCreateWithFlags(&sim->ev_fork, cudaEventDisableTiming), "event");
     }
-    return LeanStreams{sim->stream, {sim->side[0], sim->side[1]}, sim->ev_fork, {sim->ev_join[0], sim->ev_join[1]}};
+    LeanStreams ls;
+    ls.main = sim->stream;
+    ls.fork = sim->ev_fork;
+    for (int q = 0; q < LEAN_STREAMS; ++q) ls.side[q] = sim->side[q], ls.join[q] = sim->ev_join[q];
+    return ls;
 }
 
+// One step.  The single-pass schedules alternate the ping-pong buffers; the
+// host mirror of the parity (sim->cur) flips with every launched step.
 template <typename real>
 cudaError_t launch_one(sj_sim* sim) {
     auto& dv = devv<real>(sim);
     const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
-    if (sim->schedule == SJ_SCHED_FUSED)
-        return launch_lean_step<real>(dv.data(), sim->n_inst, sim->l_zb, 0, sim->d_state, lean_streams(sim));
-    if (sim->schedule == SJ_SCHED_TMA) {
+    cudaError_t e;
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        prepare_lean<real>(sim);
+        e = launch_lean_step<real>(dv.data(), sim->ltiles.data(), sim->n_inst, sim->l_zb, 0, sim->cur, sim->d_state,
+                                   lean_streams(sim));
+    } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
-        return launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
+        e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
+    } else {
+        return launch_split_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream);
     }
-    return launch_split_step<real>(d, dv.data(), sim->n_inst, sim->d_state, sim->stream);
+    sim->cur ^= 1;
+    return e;
 }
 
 // Time `steps` dry launches (no state change) of every tiling candidate and
@@ -806,10 +854,13 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
     const auto& dv = devv<real>(sim);
     const LeanStreams ls = lean_streams(sim);
     for (int zb : zbs) {
-        ck(launch_lean_step<real>(dv.data(), sim->n_inst, zb, 1, sim->d_state, ls), "autotune");
+        sim->l_zb = zb;
+        prepare_lean<real>(sim);
+        const LeanTiles* lt = sim->ltiles.data();
+        ck(launch_lean_step<real>(dv.data(), lt, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls), "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
-            ck(launch_lean_step<real>(dv.data(), sim->n_inst, zb, 1, sim->d_state, ls), "autotune");
+            ck(launch_lean_step<real>(dv.data(), lt, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls), "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
         float ms = 0;
@@ -822,6 +873,7 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     sim->l_zb = bzb;
+    prepare_lean<real>(sim);
     if (best_zs) *best_zs = bzb;
     if (best_ms) *best_ms = best / steps;
 }
@@ -890,53 +942,58 @@ void do_steps(sj_sim* sim, long long n) {
     ensure_capacity<real>(sim, sim->t + n);
     for (long long q = 0; q < n; ++q) ck(launch_one<real>(sim), "step launch");
     sim->t += n;
-    if (sim->schedule != SJ_SCHED_SPLIT && (n & 1)) sim->cur ^= 1;
 }
 
+// Steps in graph replays of `chunk` steps.  The single-pass schedules bake
+// the parity into their launches, so a chunk is captured once per starting
+// parity it is replayed at (one graph for even chunks, two for odd ones).
 template <typename real>
 void do_steps_graph(sj_sim* sim, long long n, int chunk) {
     if (chunk < 1) fail(SJ_E_INVALID, "chunk must be >= 1");
     ensure_capacity<real>(sim, sim->t + n);
     // everything that allocates or copies happens before the capture
     prepare_schedule<real>(sim);
-    if (!sim->graph || sim->graph_chunk != chunk || sim->graph_sched != sim->schedule ||
-        sim->graph_version != sim->table_version) {
-        if (sim->graph) cudaGraphExecDestroy(sim->graph);
-        sim->graph = nullptr;
-        cudaStream_t cs;
-        ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
-        cudaStream_t saved = sim->stream;
-        sim->stream = cs;
-        cudaGraph_t gr = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            try {
-                for (int q = 0; q < chunk && e == cudaSuccess; ++q) e = launch_one<real>(sim);
-            } catch (...) {
-                e = cudaErrorStreamCaptureInvalidated;
-            }
-            cudaError_t e2 = cudaStreamEndCapture(cs, &gr);
-            if (e == cudaSuccess) e = e2;
-        }
-        sim->stream = saved;
-        cudaStreamDestroy(cs);
-        if (e != cudaSuccess && gr) cudaGraphDestroy(gr);
-        ck(e, "graph capture");
-        e = cudaGraphInstantiate(&sim->graph, gr, 0);
-        cudaGraphDestroy(gr);
-        ck(e, "graph instantiate");
-        sim->graph_chunk = chunk;
-        sim->graph_sched = sim->schedule;
-        sim->graph_version = sim->table_version;
-    }
+    if (sim->graph_chunk != chunk || sim->graph_sched != sim->schedule || sim->graph_version != sim->table_version)
+        sim->drop_graphs();
+    sim->graph_chunk = chunk;
+    sim->graph_sched = sim->schedule;
+    sim->graph_version = sim->table_version;
+    const bool flips = sim->schedule != SJ_SCHED_SPLIT;
     long long left = n;
     while (left >= chunk) {
-        ck(cudaGraphLaunch(sim->graph, sim->stream), "graph launch");
+        const int p = flips ? sim->cur : 0;
+        if (!sim->graph[p]) {
+            cudaStream_t cs;
+            ck(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+            cudaStream_t saved = sim->stream;
+            const int saved_cur = sim->cur;
+            sim->stream = cs;
+            cudaGraph_t gr = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                try {
+                    for (int q = 0; q < chunk && e == cudaSuccess; ++q) e = launch_one<real>(sim);
+                } catch (...) {
+                    e = cudaErrorStreamCaptureInvalidated;
+                }
+                cudaError_t e2 = cudaStreamEndCapture(cs, &gr);
+                if (e == cudaSuccess) e = e2;
+            }
+            sim->stream = saved;
+            sim->cur = saved_cur;  // capturing ran nothing
+            cudaStreamDestroy(cs);
+            if (e != cudaSuccess && gr) cudaGraphDestroy(gr);
+            ck(e, "graph capture");
+            e = cudaGraphInstantiate(&sim->graph[p], gr, 0);
+            cudaGraphDestroy(gr);
+            ck(e, "graph instantiate");
+        }
+        ck(cudaGraphLaunch(sim->graph[p], sim->stream), "graph launch");
+        if (flips && (chunk & 1)) sim->cur ^= 1;
         left -= chunk;
     }
     for (long long q = 0; q < left; ++q) ck(launch_one<real>(sim), "step launch");
     sim->t += n;
-    if (sim->schedule != SJ_SCHED_SPLIT && (n & 1)) sim->cur ^= 1;
 }
 
 int finish(sj_sim* sim, int code, const std::string& msg) {
@@ -1102,10 +1159,7 @@ int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {
         if (zseg != 8 && zseg != 16 && zseg != 32 && zseg != 64)
             return finish(sim, SJ_E_INVALID, "fused schedule: zseg must be 8, 16, 32 or 64");
         sim->l_zb = zseg;
-        if (sim->graph) {
-            cudaGraphExecDestroy(sim->graph);
-            sim->graph = nullptr;
-        }
+        sim->drop_graphs();
         return SJ_OK;
     }
     const int sb = sim->precision == SJ_F64 ? fused_smem_bytes<double>(tile_y, ring)
@@ -1117,10 +1171,7 @@ int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {
     sim->f_ring = ring;
     sim->f_zs = zseg;
     sim->fused_ready = false;
-    if (sim->graph) {
-        cudaGraphExecDestroy(sim->graph);
-        sim->graph = nullptr;
-    }
+    sim->drop_graphs();
     return SJ_OK;
 }
 
@@ -1142,10 +1193,7 @@ int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* ring, int3
                 float* ms_per_step) {
     if (!sim || steps < 1) return SJ_E_INVALID;
     SJ_TRY(sim)
-    if (sim->graph) {
-        cudaGraphExecDestroy(sim->graph);
-        sim->graph = nullptr;
-    }
+    sim->drop_graphs();
     if (sim->precision == SJ_F64)
         autotune<double>(sim, steps, tile_y, ring, zseg, ms_per_step);
     else
@@ -1207,9 +1255,19 @@ int64_t sj_voxels(const sj_sim* sim, int32_t inst) { INST_GET(voxels, -1) }
 double sj_bytes_per_step(const sj_sim* sim, int32_t inst) { INST_GET(bytes_per_step, NAN) }
 int32_t sj_launches_per_step(const sj_sim* sim) {
     if (!sim) return -1;
-    if (sim->schedule == SJ_SCHED_FUSED)
-        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), sim->n_inst, sim->l_zb)
-                                        : lean_launches(sim->h32.data(), sim->n_inst, sim->l_zb);
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        // counts from the tile classification (the lists need not be on the device yet)
+        std::vector<LeanTiles> lt(sim->n_inst);
+        std::vector<unsigned> lists[LEAN_CLASSES];
+        for (int q = 0; q < sim->n_inst; ++q) {
+            const int r = sim->precision == SJ_F64 ? lean_classify(sim->h64[q], sim->l_zb, lists)
+                                                   : lean_classify(sim->h32[q], sim->l_zb, lists);
+            if (r != 0) return -1;
+            for (int c = 0; c < LEAN_CLASSES; ++c) lt[q].count[c] = (long long)lists[c].size();
+        }
+        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), sim->n_inst)
+                                        : lean_launches(sim->h32.data(), lt.data(), sim->n_inst);
+    }
     if (sim->schedule == SJ_SCHED_TMA) return 1;
     int maxp = 0;
     for (int q = 0; q < sim->n_inst; ++q)

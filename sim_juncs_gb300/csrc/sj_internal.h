@@ -2,6 +2,7 @@
 // kernels (sj_step.cu, sj_raster.cu).  Nothing here crosses the C ABI.
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 #include "../../include/sj.h"
 
@@ -107,38 +108,44 @@ struct FusedLaunch {
 template <typename real>
 cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState* st,
                               const FusedLaunch& fl, cudaStream_t s);
-// Fused (lean) schedule: each launch carries its instance descriptors as a
-// kernel parameter; a step is a general-, a single-slab- and a plain-tile
-// launch per group of at most LEAN_TAB instances, and the last block of all
-// of them advances the step counter.
-constexpr int LEAN_TAB = 32;
-template <typename real, int K>
-struct LeanTable {
-    int n_inst;                 // descriptors used, <= K
-    int dry;                    // 1 = time only: no step advance, no in-place stores
-    unsigned step_blocks;       // blocks of all launches of the step
-    int any_slab;               // some instance has CPML slabs
-    long long n_items;          // tiles (one block each); probe blocks follow them in k_lean_general
-    long long item_pre[K + 1];  // prefix of tiles per instance (all tiles)
-    long long plain_pre[K + 1]; // prefix of plain-box tiles per instance
-    long long probe_pre[K + 1]; // prefix of probe blocks per instance
-    int box[K][6];              // plain box in tile coordinates: x0, x1, y0, y1, z0, z1
-    InstDev<real> inst[K];
-};
-long long lean_items(int nx, int ny, int nz, int zb);  // stepping blocks of one instance
+// Fused (lean) schedule.  Tiles (32 x 8 columns x zb planes) fall into four
+// classes by what their footprint touches: CPML slabs of no axis (plain),
+// of one axis (slab) or of several (multi), or a source or dispersive voxel
+// (general).  Each step is one launch per instance and non-empty class; the
+// launch carries the instance descriptor as a kernel parameter.
+enum { LEAN_PLAIN = 0, LEAN_SLAB = 1, LEAN_MULTI = 2, LEAN_GENERAL = 3, LEAN_CLASSES = 4 };
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, int n_inst, int zb);  // launches per step
-// Streams of one fused step: the general kernel runs on `main`, the
-// single-slab and plain kernels on the side streams, forked from and joined
-// back into `main` with the events (side streams null: all on `main`).
+struct LeanTable {
+    InstDev<real> inst;         // slot 0 of F / psiH = current buffers, slot 1 = next
+    const unsigned* tiles;      // device list: tx | ty << 9 | tz << 19 | slab mask << 29
+    long long n_tiles;          // tiles of this launch (general: probe blocks follow)
+    int dry;                    // 1 = time only: no step advance, no in-place stores
+    unsigned step_blocks;       // general-launch blocks of the whole step
+};
+// Device tile lists of one instance, by class.
+struct LeanTiles {
+    const unsigned* list[LEAN_CLASSES];
+    long long count[LEAN_CLASSES];
+};
+long long lean_items(int nx, int ny, int nz, int zb);  // tiles of one instance
+template <typename real>
+int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists);  // -1: grid too large
+template <typename real>
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst);  // launches per step
+// Streams of one fused step: LEAN_SETS sets of one stream per tile class,
+// forked from `main` and joined back into it with the events; instance q's
+// launches go to set q % LEAN_SETS, so the small launches of many instances
+// overlap (side streams null: all on `main`).
+constexpr int LEAN_SETS = 4;
+constexpr int LEAN_STREAMS = LEAN_SETS * LEAN_CLASSES;
 struct LeanStreams {
     cudaStream_t main;
-    cudaStream_t side[2];
-    cudaEvent_t fork, join[2];
+    cudaStream_t side[LEAN_STREAMS];
+    cudaEvent_t fork, join[LEAN_STREAMS];
 };
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, int n_inst, int zb, int dry, DevState* st,
-                             const LeanStreams& ls);
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst, int zb, int dry,
+                             int cur, DevState* st, const LeanStreams& ls);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>

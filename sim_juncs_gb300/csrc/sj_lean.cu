@@ -16,18 +16,21 @@
 // CPML psi) make the recomputation race-free: nothing a block reads is
 // written during the step.
 //
-// Three kernels share the tiles of a step, by what a tile's footprint (own
-// cells and the recomputed x-1/y-1/z-1 neighbours) touches.  k_lean_plain
-// takes tiles clear of CPML slabs, sources and dispersive voxels: a short
-// loop that keeps few registers and runs at high occupancy.  k_lean_slab
-// takes tiles in the slabs of exactly one axis (most of the CPML volume),
-// compiled per axis so the other axes' terms vanish.  k_lean_general takes
-// the rest (slab edges and corners, sources, polarisations) and the probe
-// blocks.  The three run concurrently on forked streams, and the last block
-// of the step, whichever kernel it belongs to, advances the step counter.
-// All evaluate one update
-// formula, so a voxel's result does not depend on which kernel (or which
-// tiling) updated it:
+// Four kernels share the tiles of a step, by what a tile's footprint (own
+// cells and the recomputed x-1/y-1/z-1 neighbours) touches; the host sorts
+// the tiles into one list per class.  k_lean_plain takes tiles clear of CPML
+// slabs, sources and dispersive voxels: a short loop that keeps few
+// registers and runs at high occupancy.  k_lean_slab takes tiles in the
+// slabs of exactly one axis (most of the CPML volume) and k_lean_multi those
+// in the slabs of two or three (edges, corners), both compiled per axis set
+// so the other axes' terms vanish.  k_lean_general takes tiles with a source
+// or dispersive voxel and the probe blocks; its blocks (the only ones that
+// read the step counter) count themselves, and the last one advances the
+// step.  A step launches each non-empty class of each instance on streams
+// forked from the caller's (one per class and instance set), so the kernels
+// overlap.  All
+// evaluate one update formula, so a voxel's result does not depend on which
+// kernel (or which tiling) updated it:
 //   H^{n+1/2} = fma(-S, curl E, H^{n-1/2}) [- dt J_H]
 //   E^{n+1}   = fma(S ε∞⁻¹, curl H, E^n) [then fma(-ε∞⁻¹, dt J + Σ_p ΔP_p, ·)]
 // with curl including the CPML ψ terms.  This file is compiled with
@@ -50,6 +53,9 @@ constexpr int LMAXF = 256;
 #ifndef SJ_LEAN_SLAB_MINB
 #define SJ_LEAN_SLAB_MINB 4
 #endif
+#ifndef SJ_LEAN_MULTI_MINB
+#define SJ_LEAN_MULTI_MINB 3
+#endif
 #ifndef SJ_LEAN_GEN_MINB
 #define SJ_LEAN_GEN_MINB 3
 #endif
@@ -58,11 +64,27 @@ constexpr int plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PLAIN_MINB : 3; 
 template <typename real>
 constexpr int slab_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB_MINB : 2; }
 template <typename real>
+constexpr int multi_minb() { return sizeof(real) == 4 ? SJ_LEAN_MULTI_MINB : 2; }
+template <typename real>
 constexpr int general_minb() { return sizeof(real) == 4 ? SJ_LEAN_GEN_MINB : 2; }
 
 // Reads of buffer `cur` (fields, H-side psi), profiles and material tables
 // go through the non-coherent path: nothing writes them during the step, and
 // the compiler may then move them ahead of the stores of the previous plane.
+// L2 prefetch distance (planes): lane 0 of each warp (one 32-column row of
+// a tile) asks the TMA unit to bring the row of plane k + LEAN_PF of every
+// array the step reads into L2, so the loads of that plane find it there.
+#ifndef SJ_LEAN_PF
+#define SJ_LEAN_PF 2
+#endif
+constexpr int LEAN_PF = SJ_LEAN_PF;
+
+// one 32-element row at p (16-byte aligned: rows start on 128-byte boundaries)
+template <typename T>
+__device__ __forceinline__ void prefetch_row(const T* p) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "n"(32 * sizeof(T)));
+}
+
 template <typename real>
 __device__ __forceinline__ real ldg(const real* p, long long o) {
     return __ldg(p + o);
@@ -72,14 +94,17 @@ __device__ __forceinline__ real ldz(const real* p, long long o, bool ok) {
     return ok ? __ldg(p + o) : real(0);
 }
 
+__host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ inline int imin(int a, int b) { return a < b ? a : b; }
+
 // Does the tile's footprint touch a source (own cells and the x-1 / y-1 /
 // z-1 neighbours whose H it recomputes), or do its own cells touch the
 // bounding box of the dispersive voxels?  Block-uniform.
 template <typename real>
-__device__ __forceinline__ bool tile_has_extras(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
-    const int xa = max(i0 - 1, 0), xb = min(i0 + LX, I.nx) - 1;
-    const int ya = max(j0 - 1, 0), yb = min(j0 + LY, I.ny) - 1;
-    const int za = max(z0 - 1, 0), zb = z1 - 1;
+__host__ __device__ inline bool tile_has_extras(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
+    const int xa = imax(i0 - 1, 0), xb = imin(i0 + LX, I.nx) - 1;
+    const int ya = imax(j0 - 1, 0), yb = imin(j0 + LY, I.ny) - 1;
+    const int za = imax(z0 - 1, 0), zb = z1 - 1;
     for (int q = 0; q < I.n_src; ++q) {
         const SrcDev<real>& sv = I.src[q];
         if (sv.lo[0] <= xb && sv.lo[0] + sv.n[0] > xa && sv.lo[1] <= yb && sv.lo[1] + sv.n[1] > ya &&
@@ -94,23 +119,23 @@ __device__ __forceinline__ bool tile_has_extras(const InstDev<real>& I, int i0, 
 
 // ------------------------------------------------------------- plain tiles
 template <typename real, int ZB>
-__device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int ty, int tz, int cur) {
+__device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int ty, int tz) {
     const int i = tx * LX + threadIdx.x, j = ty * LY + threadIdx.y;
     const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
     if (i >= I.nx || j >= I.ny) return;
     const long long px = I.px, plane = I.plane;
-    const real* eX = I.F[cur][0];
-    const real* eY = I.F[cur][1];
-    const real* eZ = I.F[cur][2];
-    const real* hX = I.F[cur][3];
-    const real* hY = I.F[cur][4];
-    const real* hZ = I.F[cur][5];
-    real* oEX = I.F[cur ^ 1][0];
-    real* oEY = I.F[cur ^ 1][1];
-    real* oEZ = I.F[cur ^ 1][2];
-    real* oHX = I.F[cur ^ 1][3];
-    real* oHY = I.F[cur ^ 1][4];
-    real* oHZ = I.F[cur ^ 1][5];
+    const real* eX = I.F[0][0];
+    const real* eY = I.F[0][1];
+    const real* eZ = I.F[0][2];
+    const real* hX = I.F[0][3];
+    const real* hY = I.F[0][4];
+    const real* hZ = I.F[0][5];
+    real* oEX = I.F[1][0];
+    real* oEY = I.F[1][1];
+    real* oEZ = I.F[1][2];
+    real* oHX = I.F[1][3];
+    real* oHY = I.F[1][4];
+    real* oHZ = I.F[1][5];
     const real S = I.S;
     const bool xm = i > 0, ym = j > 0, xp = i + 1 < I.nx, yp = j + 1 < I.ny;
 
@@ -119,8 +144,19 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;
+    const long long orow = o - threadIdx.x;  // row start of this warp at plane k
     for (; k < z1; ++k, o += plane) {
         const bool kp = k + 1 < I.nz;
+        if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < I.nz && k + LEAN_PF < z1) {
+            const long long r = orow + (long long)(k - (z0 > 0 ? z0 - 1 : 0) + 1 + LEAN_PF) * plane;
+            prefetch_row(eX + r);
+            prefetch_row(eY + r);
+            prefetch_row(eZ + r);
+            prefetch_row(hX + r);
+            prefetch_row(hY + r);
+            prefetch_row(hZ + r);
+            prefetch_row(I.combo + r);
+        }
         const real ex_n = ldz(eX, o + plane, kp), ey_n = ldz(eY, o + plane, kp);
         const real exm_n = ldz(eX, o + plane - 1, kp && xm), eym_n = ldz(eY, o + plane - px, kp && ym);
         const real ez = ldg(eZ, o);
@@ -234,11 +270,11 @@ __device__ __forceinline__ real e_new(const InstDev<real>& I, int i, int j, int 
 // Slab axes a tile's footprint touches (bit a = axis a): the same footprint
 // test as the host's plain box.
 template <typename real>
-__device__ __forceinline__ int tile_slab_mask(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
+__host__ __device__ inline int tile_slab_mask(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
     int m = 0;
-    if (!(max(i0 - 1, 0) >= I.pl[0] && min(i0 + LX, I.nx) - 1 < I.nx - I.ph[0])) m |= 1;
-    if (!(max(j0 - 1, 0) >= I.pl[1] && min(j0 + LY, I.ny) - 1 < I.ny - I.ph[1])) m |= 2;
-    if (!(max(z0 - 1, 0) >= I.pl[2] && z1 - 1 < I.nz - I.ph[2])) m |= 4;
+    if (!(imax(i0 - 1, 0) >= I.pl[0] && imin(i0 + LX, I.nx) - 1 < I.nx - I.ph[0])) m |= 1;
+    if (!(imax(j0 - 1, 0) >= I.pl[1] && imin(j0 + LY, I.ny) - 1 < I.ny - I.ph[1])) m |= 2;
+    if (!(imax(z0 - 1, 0) >= I.pl[2] && z1 - 1 < I.nz - I.ph[2])) m |= 4;
     return m;
 }
 
@@ -246,8 +282,7 @@ __device__ __forceinline__ int tile_slab_mask(const InstDev<real>& I, int i0, in
 // and, with EXTRAS, sources and polarisations.  The x and y profile values of
 // the column are loaded once; z values once per plane.
 template <typename real, int ZB, int MASK, bool EXTRAS>
-__device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int ty, int tz, long long n, int cur,
-                                           bool dry) {
+__device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int ty, int tz, long long n, bool dry) {
     constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
     const int i = tx * LX + threadIdx.x, j = ty * LY + threadIdx.y;
     const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
@@ -255,25 +290,25 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
 
     const int nx = I.nx, ny = I.ny, nz = I.nz;
     const long long px = I.px, plane = I.plane, vol = I.vol;
-    const real* eX = I.F[cur][0];
-    const real* eY = I.F[cur][1];
-    const real* eZ = I.F[cur][2];
-    const real* hX = I.F[cur][3];
-    const real* hY = I.F[cur][4];
-    const real* hZ = I.F[cur][5];
-    real* oEX = I.F[cur ^ 1][0];
-    real* oEY = I.F[cur ^ 1][1];
-    real* oEZ = I.F[cur ^ 1][2];
-    real* oHX = I.F[cur ^ 1][3];
-    real* oHY = I.F[cur ^ 1][4];
-    real* oHZ = I.F[cur ^ 1][5];
+    const real* eX = I.F[0][0];
+    const real* eY = I.F[0][1];
+    const real* eZ = I.F[0][2];
+    const real* hX = I.F[0][3];
+    const real* hY = I.F[0][4];
+    const real* hZ = I.F[0][5];
+    real* oEX = I.F[1][0];
+    real* oEY = I.F[1][1];
+    real* oEZ = I.F[1][2];
+    real* oHX = I.F[1][3];
+    real* oHY = I.F[1][4];
+    real* oHZ = I.F[1][5];
     // psi of axis a: slot p at psi[a] + p * vol (H side ping-pong, E side in place)
-    const real* hiX = SX ? I.psiH[cur][0] : nullptr;
-    const real* hiY = SY ? I.psiH[cur][1] : nullptr;
-    const real* hiZ = SZ ? I.psiH[cur][2] : nullptr;
-    real* hoX = SX ? I.psiH[cur ^ 1][0] : nullptr;
-    real* hoY = SY ? I.psiH[cur ^ 1][1] : nullptr;
-    real* hoZ = SZ ? I.psiH[cur ^ 1][2] : nullptr;
+    const real* hiX = SX ? I.psiH[0][0] : nullptr;
+    const real* hiY = SY ? I.psiH[0][1] : nullptr;
+    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
+    real* hoX = SX ? I.psiH[1][0] : nullptr;
+    real* hoY = SY ? I.psiH[1][1] : nullptr;
+    real* hoZ = SZ ? I.psiH[1][2] : nullptr;
     real* peX = SX ? I.psiE[0] : nullptr;
     real* peY = SY ? I.psiE[1] : nullptr;
     real* peZ = SZ ? I.psiE[2] : nullptr;
@@ -310,10 +345,39 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;  // H^{n+1/2} of plane k-1 at the own cell
+    const long long orow = o - threadIdx.x;  // row start of this warp at plane k
+    const int k0 = k;
+    // the x psi rows are prefetched only where the tile touches an x slab
+    // (the arrays exist only for axes with slabs)
+    const int i0 = tx * LX;
+    const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
     for (; k < z1; ++k, o += plane) {
         const bool kp = k + 1 < nz;
         const bool store = k >= z0;
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
+        if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < nz && k + LEAN_PF < z1) {
+            const int kq = k + 1 + LEAN_PF;
+            const long long r = orow + (long long)(kq - k0) * plane;
+            prefetch_row(eX + r);
+            prefetch_row(eY + r);
+            prefetch_row(eZ + r);
+            prefetch_row(hX + r);
+            prefetch_row(hY + r);
+            prefetch_row(hZ + r);
+            prefetch_row(I.combo + r);
+            if (xt) {
+                prefetch_row(hiX + r), prefetch_row(hiX + vol + r);
+                prefetch_row(peX + r), prefetch_row(peX + vol + r);
+            }
+            if (SY && yo) {
+                prefetch_row(hiY + r), prefetch_row(hiY + vol + r);
+                prefetch_row(peY + r), prefetch_row(peY + vol + r);
+            }
+            if (SZ && (kq < I.pl[2] || kq >= nz - I.ph[2])) {
+                prefetch_row(hiZ + r), prefetch_row(hiZ + vol + r);
+                prefetch_row(peZ + r), prefetch_row(peZ + vol + r);
+            }
+        }
         real bzi = 1, czi = 0, bzh = 1, czh = 0;
         if (zo) {
             const real* pr = I.prof[2];
@@ -482,30 +546,26 @@ __device__ __forceinline__ void lean_probe_block(const InstDev<real>& I, long lo
     }
 }
 
-__device__ __forceinline__ int lean_find(const long long* pre, int n, long long b) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (pre[mid] <= b)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
+// The instance descriptor travels in the launch's parameter space
+// (__grid_constant__), with slot 0 of the ping-pong pairs (fields, H-side
+// psi) holding the current buffers and slot 1 the next ones: the host swaps
+// them by parity.  Every block reads the descriptor through the constant
+// cache at fixed offsets, so pointers, extents and coefficients cost no
+// per-thread registers.  Each launch takes one instance and one tile class;
+// its blocks map to the class's tiles through a list built on the host.
+
+__device__ __forceinline__ void tile_decode(unsigned code, int& tx, int& ty, int& tz, int& mask) {
+    tx = (int)(code & 511u);
+    ty = (int)((code >> 9) & 1023u);
+    tz = (int)((code >> 19) & 1023u);
+    mask = (int)(code >> 29);
 }
 
-// The instance descriptors travel in the launch's parameter space
-// (__grid_constant__): every block reads them through the constant cache with
-// block-uniform indices, so field pointers, extents and coefficients live in
-// uniform registers instead of taking per-thread registers, which a
-// descriptor table in global memory would.
-
-// Every block of every launch of a step counts itself; the last one (of
-// step_blocks) advances the step and flips the buffers.  The launches of a
-// step may run concurrently: each block reads `cur` before it counts, so no
-// block can see the flip of its own step.
-template <typename real, int K>
-__device__ __forceinline__ void finish_block(const LeanTable<real, K>& tab, DevState* st) {
+// Only the general launches read the step counter (sources, probes): their
+// blocks count themselves, and the last one of the step advances the step
+// and flips the device copy of the parity.
+template <typename real>
+__device__ __forceinline__ void finish_block(const LeanTable<real>& tab, DevState* st) {
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         __threadfence();
@@ -521,86 +581,60 @@ __device__ __forceinline__ void finish_block(const LeanTable<real, K>& tab, DevS
     }
 }
 
-// Plain tiles: block -> tile of the instance's plain box; tiles whose
-// footprint holds a source or dispersive voxel are left to k_lean_general.
-template <typename real, int ZB, int K>
+// Plain tiles: no CPML slab, source or dispersive voxel in the footprint.
+template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, plain_minb<real>())
-k_lean_plain(const __grid_constant__ LeanTable<real, K> tab, DevState* st) {
-    const int cur = st->cur;
-    const long long b = blockIdx.x;
-    const int ii = K == 1 ? 0 : lean_find(tab.plain_pre, tab.n_inst, b);
-    const InstDev<real>& I = tab.inst[ii];
-    const int* bx = tab.box[ii];
-    const int bnx = bx[1] - bx[0], bny = bx[3] - bx[2];
-    const long long local = b - tab.plain_pre[ii];
-    const int tx = bx[0] + (int)(local % bnx);
-    const int ty = bx[2] + (int)((local / bnx) % bny);
-    const int tz = bx[4] + (int)(local / ((long long)bnx * bny));
-    const int z0 = tz * ZB;
-    // plain_block returns early for columns outside the grid; every thread
-    // still reaches the barrier in finish_block
-    if (!tile_has_extras(I, tx * LX, ty * LY, z0, min(I.nz, z0 + ZB))) plain_block<real, ZB>(I, tx, ty, tz, cur);
-    finish_block(tab, st);
+k_lean_plain(const __grid_constant__ LeanTable<real> tab) {
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    plain_block<real, ZB>(tab.inst, tx, ty, tz);
 }
 
-// Tile of block b among all tiles of an instance (x fastest, then y, z).
-template <typename real>
-__device__ __forceinline__ void tile_of(const InstDev<real>& I, long long local, int& tx, int& ty, int& tz) {
-    const int ntx = (I.nx + LX - 1) / LX, nty = (I.ny + LY - 1) / LY;
-    tx = (int)(local % ntx);
-    ty = (int)((local / ntx) % nty);
-    tz = (int)(local / ((long long)ntx * nty));
-}
-
-// Single-slab tiles: the footprint touches the slabs of exactly one axis and
-// holds no source or dispersive voxel.  Every tile gets a block; the others
-// only count themselves.
-template <typename real, int ZB, int K>
+// Single-slab tiles: the footprint touches the slabs of exactly one axis.
+template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, slab_minb<real>())
-k_lean_slab(const __grid_constant__ LeanTable<real, K> tab, DevState* st) {
-    const int cur = st->cur;
-    const long long b = blockIdx.x;
-    const int ii = K == 1 ? 0 : lean_find(tab.item_pre, tab.n_inst, b);
-    const InstDev<real>& I = tab.inst[ii];
-    int tx, ty, tz;
-    tile_of(I, b - tab.item_pre[ii], tx, ty, tz);
-    const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
-    const int m = tile_slab_mask(I, tx * LX, ty * LY, z0, z1);
-    if ((m == 1 || m == 2 || m == 4) && !tile_has_extras(I, tx * LX, ty * LY, z0, z1)) {
-        if (m == 1)
-            tile_block<real, ZB, 1, false>(I, tx, ty, tz, 0, cur, tab.dry != 0);
-        else if (m == 2)
-            tile_block<real, ZB, 2, false>(I, tx, ty, tz, 0, cur, tab.dry != 0);
-        else
-            tile_block<real, ZB, 4, false>(I, tx, ty, tz, 0, cur, tab.dry != 0);
-    }
-    finish_block(tab, st);
+k_lean_slab(const __grid_constant__ LeanTable<real> tab) {
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    if (m == 1)
+        tile_block<real, ZB, 1, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+    else if (m == 2)
+        tile_block<real, ZB, 2, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+    else
+        tile_block<real, ZB, 4, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
 }
 
-// General tiles (several slab axes, or a source or dispersive voxel in the
-// footprint), then the probe blocks.
-template <typename real, int ZB, int K>
+// Multi-slab tiles: the slabs of two or three axes (edges and corners).
+template <typename real, int ZB>
+__global__ void __launch_bounds__(LX * LY, multi_minb<real>())
+k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    if (m == 3)
+        tile_block<real, ZB, 3, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+    else if (m == 5)
+        tile_block<real, ZB, 5, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+    else if (m == 6)
+        tile_block<real, ZB, 6, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+    else
+        tile_block<real, ZB, 7, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+}
+
+// General tiles (a source or dispersive voxel in the footprint), then the
+// probe blocks.
+template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, general_minb<real>())
-k_lean_general(const __grid_constant__ LeanTable<real, K> tab, DevState* st) {
+k_lean_general(const __grid_constant__ LeanTable<real> tab, DevState* st) {
     const long long n = st->step;
-    const int cur = st->cur;
     const long long b = blockIdx.x;
-    if (b < tab.n_items) {
-        const int ii = K == 1 ? 0 : lean_find(tab.item_pre, tab.n_inst, b);
-        const InstDev<real>& I = tab.inst[ii];
-        int tx, ty, tz;
-        tile_of(I, b - tab.item_pre[ii], tx, ty, tz);
-        const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
-        const int m = tile_slab_mask(I, tx * LX, ty * LY, z0, z1);
-        const bool ext = tile_has_extras(I, tx * LX, ty * LY, z0, z1);
+    if (b < tab.n_tiles) {
+        int tx, ty, tz, m;
+        tile_decode(__ldg(tab.tiles + b), tx, ty, tz, m);
         // tile_block returns early for columns outside the grid; every
-        // thread still reaches the barrier below
-        if (ext || (m != 0 && m != 1 && m != 2 && m != 4))
-            tile_block<real, ZB, 7, true>(I, tx, ty, tz, n, cur, tab.dry != 0);
+        // thread still reaches the barrier in finish_block
+        tile_block<real, ZB, 7, true>(tab.inst, tx, ty, tz, n, tab.dry != 0);
     } else if (!tab.dry) {
-        const long long pb = b - tab.n_items;
-        const int ii = K == 1 ? 0 : lean_find(tab.probe_pre, tab.n_inst, pb);
-        lean_probe_block<real>(tab.inst[ii], pb - tab.probe_pre[ii], n, cur, st);
+        lean_probe_block<real>(tab.inst, b - tab.n_tiles, n, 0, st);
     }
     finish_block(tab, st);
 }
@@ -609,135 +643,112 @@ long long lean_items(int nx, int ny, int nz, int zb) {
     return (long long)((nx + LX - 1) / LX) * ((ny + LY - 1) / LY) * ((nz + zb - 1) / zb);
 }
 
+template <typename real>
+int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists) {
+    const int ntx = (I.nx + LX - 1) / LX, nty = (I.ny + LY - 1) / LY, ntz = (I.nz + zb - 1) / zb;
+    if (ntx > 512 || nty > 1024 || ntz > 1024) return -1;
+    for (int c = 0; c < LEAN_CLASSES; ++c) lists[c].clear();
+    for (int tz = 0; tz < ntz; ++tz)
+        for (int ty = 0; ty < nty; ++ty)
+            for (int tx = 0; tx < ntx; ++tx) {
+                const int i0 = tx * LX, j0 = ty * LY, z0 = tz * zb, z1 = imin(I.nz, z0 + zb);
+                const int m = tile_slab_mask(I, i0, j0, z0, z1);
+                const int c = tile_has_extras(I, i0, j0, z0, z1) ? LEAN_GENERAL
+                              : m == 0                           ? LEAN_PLAIN
+                              : (m == 1 || m == 2 || m == 4)     ? LEAN_SLAB
+                                                                 : LEAN_MULTI;
+                lists[c].push_back((unsigned)tx | ((unsigned)ty << 9) | ((unsigned)tz << 19) | ((unsigned)m << 29));
+            }
+    return 0;
+}
+template int lean_classify<float>(const InstDev<float>&, int, std::vector<unsigned>*);
+template int lean_classify<double>(const InstDev<double>&, int, std::vector<unsigned>*);
+
 namespace {
 
-// Tiles [t0, t1) along one axis whose footprint [max(lo-1, 0), min(lo+w, n)-1]
-// (lo = t*w) stays clear of both CPML slabs [0, pl) and [n-ph, n).
-void clear_range(int n, int w, int pl, int ph, int* t0, int* t1) {
-    const int nt = (n + w - 1) / w;
-    int a = nt, b = 0;
-    for (int t = 0; t < nt; ++t) {
-        const int lo = std::max(t * w - 1, 0), hi = std::min(t * w + w, n) - 1;
-        if (lo >= pl && hi < n - ph) {
-            a = std::min(a, t);
-            b = t + 1;
-        }
-    }
-    if (a >= b) a = b = 0;
-    *t0 = a;
-    *t1 = b;
+template <typename real>
+long long probe_blocks(const InstDev<real>& I) {
+    return (I.n_probe + LX * LY - 1) / (LX * LY);
 }
 
-template <typename real, int K>
-void fill_table(LeanTable<real, K>& t, const InstDev<real>* h, int n, int zb, int dry) {
-    t.n_inst = n;
-    t.dry = dry;
-    t.step_blocks = 0;
-    t.item_pre[0] = 0;
-    t.plain_pre[0] = 0;
-    t.probe_pre[0] = 0;
-    for (int q = 0; q < n; ++q) {
-        const InstDev<real>& I = h[q];
-        t.inst[q] = I;
-        int* bx = t.box[q];
-        clear_range(I.nx, LX, I.pl[0], I.ph[0], bx + 0, bx + 1);
-        clear_range(I.ny, LY, I.pl[1], I.ph[1], bx + 2, bx + 3);
-        clear_range(I.nz, zb, I.pl[2], I.ph[2], bx + 4, bx + 5);
-        const long long plain = (long long)(bx[1] - bx[0]) * (bx[3] - bx[2]) * (bx[5] - bx[4]);
-        if (plain == 0) bx[0] = bx[1] = bx[2] = bx[3] = bx[4] = bx[5] = 0;
-        t.item_pre[q + 1] = t.item_pre[q] + lean_items(I.nx, I.ny, I.nz, zb);
-        t.plain_pre[q + 1] = t.plain_pre[q] + plain;
-        t.probe_pre[q + 1] = t.probe_pre[q] + (I.n_probe + LX * LY - 1) / (LX * LY);
-    }
-    t.n_items = t.item_pre[n];
-    t.any_slab = 0;
-    for (int q = 0; q < n; ++q)
-        for (int a = 0; a < 3; ++a) t.any_slab |= (h[q].pl[a] + h[q].ph[a]) > 0;
-}
-
-template <typename real, int K>
-long long table_blocks(const LeanTable<real, K>& t) {
-    const long long pb = t.dry ? 0 : t.plain_pre[t.n_inst];
-    return pb + (t.any_slab ? t.n_items : 0) + t.n_items + t.probe_pre[t.n_inst];
-}
-
-// General tiles on the main stream, single-slab and plain tiles on the two
-// side streams: the three kernels of a step overlap, filling each other's
-// tails.
-template <typename real, int K>
-cudaError_t launch_table(const LeanTable<real, K>& t, int zb, DevState* st, const LeanStreams& ls) {
-    const unsigned pblocks = t.dry ? 0u : (unsigned)t.plain_pre[t.n_inst];
-    const unsigned sblocks = t.any_slab ? (unsigned)t.n_items : 0u;
-    const unsigned gblocks = (unsigned)(t.n_items + t.probe_pre[t.n_inst]);
-    const dim3 block(LX, LY);
-    cudaStream_t ss = ls.side[0] ? ls.side[0] : ls.main;
-    cudaStream_t sp = ls.side[1] ? ls.side[1] : ls.main;
-#define SJ_ZB(Z)                                                                        \
-    case Z:                                                                             \
-        k_lean_general<real, Z, K><<<gblocks, block, 0, ls.main>>>(t, st);              \
-        if (sblocks) k_lean_slab<real, Z, K><<<sblocks, block, 0, ss>>>(t, st);         \
-        if (pblocks) k_lean_plain<real, Z, K><<<pblocks, block, 0, sp>>>(t, st);        \
-        break;
-    switch (zb) {  // z-segment length
-        SJ_ZB(8)
-        SJ_ZB(16)
-        SJ_ZB(32)
-        SJ_ZB(64)
-        default: return cudaErrorInvalidValue;
-    }
-#undef SJ_ZB
-    return cudaGetLastError();
+// blocks of instance q's general launch (the first instance's always has
+// at least one, so that every step has a block that advances the counter)
+template <typename real>
+long long general_blocks(const InstDev<real>& I, const LeanTiles& T, int q, int dry) {
+    const long long g = T.count[LEAN_GENERAL] + (dry ? 0 : probe_blocks(I));
+    return (q == 0 && g == 0) ? 1 : g;
 }
 
 }  // namespace
 
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, int n_inst, int zb) {
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst) {
     int total = 0;
-    for (int q0 = 0; q0 < n_inst; q0 += LEAN_TAB) {
-        const int m = std::min(LEAN_TAB, n_inst - q0);
-        static thread_local LeanTable<real, LEAN_TAB> t;
-        fill_table(t, h_insts + q0, m, zb, 0);
-        total += (t.plain_pre[m] > 0) + (t.any_slab != 0) + 1;
+    for (int q = 0; q < n_inst; ++q) {
+        for (int c = 0; c < LEAN_CLASSES; ++c)
+            if (c != LEAN_GENERAL && tiles[q].count[c] > 0) ++total;
+        if (general_blocks(h_insts[q], tiles[q], q, 0) > 0) ++total;
     }
     return total;
 }
-template int lean_launches<float>(const InstDev<float>*, int, int);
-template int lean_launches<double>(const InstDev<double>*, int, int);
+template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, int);
+template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, int);
 
+// Each class of instance q goes to its own stream of set q % LEAN_SETS: the
+// kernels of a step overlap and fill each other's tails.  Only as many sets
+// as there are instances are forked.
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, int n_inst, int zb, int dry, DevState* st,
-                             const LeanStreams& ls) {
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst, int zb, int dry,
+                             int cur, DevState* st, const LeanStreams& ls) {
     cudaError_t e = cudaSuccess;
-    const bool fork = ls.side[0] && ls.side[1];
+    const bool fork = ls.side[0] != nullptr;
+    const int nsets = fork ? std::min(n_inst, LEAN_SETS) : 0;
     if (fork) {
         e = cudaEventRecord(ls.fork, ls.main);
-        for (int q = 0; q < 2 && e == cudaSuccess; ++q) e = cudaStreamWaitEvent(ls.side[q], ls.fork, 0);
+        for (int q = 0; q < nsets * LEAN_CLASSES && e == cudaSuccess; ++q)
+            e = cudaStreamWaitEvent(ls.side[q], ls.fork, 0);
         if (e != cudaSuccess) return e;
     }
-    if (n_inst == 1) {
-        LeanTable<real, 1> t;
-        fill_table(t, h_insts, 1, zb, dry);
-        t.step_blocks = (unsigned)table_blocks(t);
-        e = launch_table(t, zb, st, ls);
-    } else {
-        // 29 KB parameter blocks: kept off the stack, one set per host thread
-        static thread_local std::vector<LeanTable<real, LEAN_TAB>> tabs;
-        const int nc = (n_inst + LEAN_TAB - 1) / LEAN_TAB;
-        if ((int)tabs.size() < nc) tabs.resize(nc);
-        long long total = 0;
-        for (int c = 0; c < nc; ++c) {
-            const int q0 = c * LEAN_TAB, m = std::min(LEAN_TAB, n_inst - q0);
-            fill_table(tabs[c], h_insts + q0, m, zb, dry);
-            total += table_blocks(tabs[c]);
+    long long gtotal = 0;
+    for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
+    const dim3 block(LX, LY);
+    for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
+        LeanTable<real> t;
+        t.inst = h_insts[q];
+        if (cur) {
+            for (int c = 0; c < 6; ++c) std::swap(t.inst.F[0][c], t.inst.F[1][c]);
+            for (int a = 0; a < 3; ++a) std::swap(t.inst.psiH[0][a], t.inst.psiH[1][a]);
         }
-        for (int c = 0; c < nc && e == cudaSuccess; ++c) {
-            tabs[c].step_blocks = (unsigned)total;
-            e = launch_table(tabs[c], zb, st, ls);
+        t.dry = dry;
+        t.step_blocks = (unsigned)gtotal;
+        const LeanTiles& T = tiles[q];
+        const long long gb = general_blocks(h_insts[q], T, q, dry);
+        cudaStream_t sc[LEAN_CLASSES];
+        for (int c = 0; c < LEAN_CLASSES; ++c)
+            sc[c] = fork ? ls.side[(q % LEAN_SETS) * LEAN_CLASSES + c] : ls.main;
+#define SJ_ZB(Z)                                                                                             \
+    case Z:                                                                                                  \
+        t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
+        if (t.n_tiles) k_lean_multi<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_MULTI]>>>(t);          \
+        t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
+        if (t.n_tiles) k_lean_slab<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_SLAB]>>>(t);            \
+        t.tiles = T.list[LEAN_GENERAL], t.n_tiles = T.count[LEAN_GENERAL];                                   \
+        if (gb) k_lean_general<real, Z><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st);                \
+        t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
+        if (t.n_tiles) k_lean_plain<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_PLAIN]>>>(t);          \
+        break;
+        switch (zb) {  // z-segment length
+            SJ_ZB(8)
+            SJ_ZB(16)
+            SJ_ZB(32)
+            SJ_ZB(64)
+            default: return cudaErrorInvalidValue;
         }
+#undef SJ_ZB
+        e = cudaGetLastError();
     }
     if (fork) {
-        for (int q = 0; q < 2 && e == cudaSuccess; ++q) {
+        for (int q = 0; q < nsets * LEAN_CLASSES && e == cudaSuccess; ++q) {
             e = cudaEventRecord(ls.join[q], ls.side[q]);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(ls.main, ls.join[q], 0);
         }
@@ -745,6 +756,8 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, int n_inst, int zb, i
     return e;
 }
 
-template cudaError_t launch_lean_step<double>(const InstDev<double>*, int, int, int, DevState*, const LeanStreams&);
-template cudaError_t launch_lean_step<float>(const InstDev<float>*, int, int, int, DevState*, const LeanStreams&);
+template cudaError_t launch_lean_step<double>(const InstDev<double>*, const LeanTiles*, int, int, int, int, DevState*,
+                                              const LeanStreams&);
+template cudaError_t launch_lean_step<float>(const InstDev<float>*, const LeanTiles*, int, int, int, int, DevState*,
+                                             const LeanStreams&);
 }  // namespace sj
