@@ -1,0 +1,256 @@
+// TEST INFRASTRUCTURE ONLY: a C-callable shim over the reference's own CGS
+// code (src/cgs_read.cpp, src/cgs_data.cpp, src/cgs.cpp, compiled unmodified
+// by `make ref` into _ref/libsjref.so).  tests/golden/make_golden.py calls
+// it to record what the reference answers; nothing in the product links it.
+//
+// It does three things a maintainer wiring bound_geom to include/sj.h does:
+//   * parse a .geom file with the reference's scene (src/cgs.cpp:577);
+//   * flatten each root composite_object into sj_csg_node postfix programs,
+//     the walk of the integration guide, reading each node's trans_mat,
+//     invert and the cylinder's squared radii (r1_sq, r2_sq), which the
+//     reference keeps non-public; the guide asks for one-line accessors,
+//     and here the standard explicit-instantiation idiom reads them;
+//   * restate parse_susceptibilities (src/disp.cpp:418-454), which lives in
+//     meep-dependent code, on the root's "susceptibilities" metadata.
+// It also exposes composite_object::in (src/cgs.cpp:431-456) itself, the
+// answer the golden vectors record.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "cgs.hpp"
+#include "cgs_read.hpp"
+#include "../include/sj.h"
+
+namespace {
+
+// Reads a non-public data member through a pointer-to-member obtained by
+// explicit template instantiation (which may name any member).
+template <typename Tag, typename Tag::type M>
+struct Reader {
+    friend typename Tag::type member_of(Tag) { return M; }
+};
+struct ObjTrans { typedef mat3x3 object::*type; friend type member_of(ObjTrans); };
+struct ObjInvert { typedef int object::*type; friend type member_of(ObjInvert); };
+struct CylR1 { typedef double cylinder::*type; friend type member_of(CylR1); };
+struct CylR2 { typedef double cylinder::*type; friend type member_of(CylR2); };
+template struct Reader<ObjTrans, &object::trans_mat>;
+template struct Reader<ObjInvert, &object::invert>;
+template struct Reader<CylR1, &cylinder::r1_sq>;
+template struct Reader<CylR2, &cylinder::r2_sq>;
+
+const mat3x3& trans_of(const object* o) { return o->*member_of(ObjTrans()); }
+int invert_of(const object* o) { return o->*member_of(ObjInvert()); }
+
+std::vector<scene*> g_scenes;
+
+void mat_copy(double* d, const mat3x3& m) {
+    for (int q = 0; q < 9; ++q) d[q] = m.el[q];
+}
+
+// acc = product of the ancestors' trans_mat (identity at the root)
+void flatten(const object* o, object_type t, const mat3x3& acc, std::vector<sj_csg_node>& out) {
+    sj_csg_node n;
+    memset(&n, 0, sizeof(n));
+    mat_copy(n.m, acc);
+    mat_copy(n.t, trans_of(o));
+    n.invert = invert_of(o);
+    switch (t) {
+        case CGS_BOX: {
+            const box* b = (const box*)o;
+            n.op = SJ_CSG_BOX;
+            vec3 c = b->get_center(), f = b->get_offset();
+            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
+            n.p[0] = f.x(), n.p[1] = f.y(), n.p[2] = f.z();
+            break;
+        }
+        case CGS_SPHERE: {
+            const sphere* s = (const sphere*)o;
+            n.op = SJ_CSG_SPHERE;
+            vec3 c = s->get_center();
+            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
+            n.p[0] = s->get_rad();
+            break;
+        }
+        case CGS_CYLINDER: {
+            const cylinder* y = (const cylinder*)o;
+            n.op = SJ_CSG_CYLINDER;
+            vec3 c = y->get_center();
+            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
+            n.p[0] = y->get_height();
+            n.p[1] = y->*member_of(CylR1());
+            n.p[2] = y->*member_of(CylR2());
+            break;
+        }
+        case CGS_PLANE: {
+            const plane* p = (const plane*)o;
+            n.op = SJ_CSG_PLANE;
+            vec3 v = p->get_normal();
+            n.p[0] = v.x(), n.p[1] = v.y(), n.p[2] = v.z(), n.p[3] = p->get_offset();
+            break;
+        }
+        default: {
+            composite_object* c = (composite_object*)o;
+            const mat3x3 inner = trans_of(o) * acc;  // children see trans_mat * r
+            if (c->get_combine_type() == CGS_CMB_NOOP) {
+                n.op = SJ_CSG_NOOP;
+                break;
+            }
+            const object* l = c->get_child_l();
+            const object* r = c->get_child_r();
+            if (l) flatten(l, c->get_child_type_l(), inner, out);
+            if (r) flatten(r, c->get_child_type_r(), inner, out);
+            // CGS_DIFFERENCE: add_child already set the right child's invert
+            n.op = (l && r) ? (c->get_combine_type() == CGS_UNION ? SJ_CSG_UNION : SJ_CSG_INTERSECT)
+                   : (l || r) ? SJ_CSG_PASS
+                              : SJ_CSG_CONST;
+        }
+    }
+    out.push_back(n);
+}
+
+// um_to_l and fs_to_t (src/disp.cpp:5-22): lengths in um and times in fs to
+// the scene's length units, scaled by the context's l_per_um
+value shim_um_to_l(context& c, cgs_func f, parse_ercode& er) {
+    value ret;
+    if (f.n_args < 1) { er = E_LACK_TOKENS; return ret; }
+    if (f.args[0].type != VAL_NUM) { er = E_BAD_TOKEN; return ret; }
+    value l_per_um = c.lookup("l_per_um");
+    if (l_per_um.type != VAL_NUM) { er = E_NOT_DEFINED; return ret; }
+    return make_val_num(l_per_um.val.x * f.args[0].val.x);
+}
+value shim_fs_to_t(context& c, cgs_func f, parse_ercode& er) {
+    value ret;
+    if (f.n_args < 1) { er = E_LACK_TOKENS; return ret; }
+    if (f.args[0].type != VAL_NUM) { er = E_BAD_TOKEN; return ret; }
+    value l_per_um = c.lookup("l_per_um");
+    if (l_per_um.type != VAL_NUM) { er = E_NOT_DEFINED; return ret; }
+    return make_val_num(0.299792458 * l_per_um.val.x * f.args[0].val.x);
+}
+
+composite_object* root_of(int h, int r) {
+    if (h < 0 || h >= (int)g_scenes.size() || !g_scenes[h]) return nullptr;
+    std::vector<composite_object*> roots = g_scenes[h]->get_roots();
+    if (r < 0 || r >= (int)roots.size()) return nullptr;
+    return roots[r];
+}
+
+}  // namespace
+
+extern "C" {
+
+// Parse a .geom file; returns a handle >= 0, or -(1 + parse_ercode) on failure.
+int sjref_load(const char* path) {
+    parse_ercode er = E_SUCCESS;
+    scene* s = new scene(path, &er);
+    if (er != E_SUCCESS) {
+        delete s;
+        return -(1 + (int)er);
+    }
+    g_scenes.push_back(s);
+    return (int)g_scenes.size() - 1;
+}
+
+// Parse with the context bound_geom gives a scene (restating
+// context_from_settings, src/disp.cpp:28-50): pi, pml_thickness, sim_length,
+// length = 2 pml + len, l_per_um, out_dir, um_to_l, fs_to_t, then the
+// user options ("name=value;..." as --opts passes them).
+int sjref_load_ctx(const char* path, double pml_thickness, double len, double um_scale, const char* opts) {
+    context con;
+    con.emplace("pi", make_val_num(M_PI));
+    con.emplace("pml_thickness", make_val_num(pml_thickness));
+    con.emplace("sim_length", make_val_num(len));
+    con.emplace("length", make_val_num(2 * pml_thickness + len));
+    con.emplace("l_per_um", make_val_num(um_scale));
+    value tmp = make_val_str(".");
+    con.emplace("out_dir", tmp);
+    cleanup_val(&tmp);
+    tmp = make_val_func("um_to_l", 1, &shim_um_to_l);
+    con.emplace("um_to_l", tmp);
+    cleanup_val(&tmp);
+    tmp = make_val_func("fs_to_t", 1, &shim_fs_to_t);
+    con.emplace("fs_to_t", tmp);
+    cleanup_val(&tmp);
+    if (opts && *opts) {
+        line_buffer lb(opts, ';');
+        con.read_from_lines(lb);
+    }
+    parse_ercode er = E_SUCCESS;
+    scene* s = new scene(path, con, &er);
+    if (er != E_SUCCESS) {
+        delete s;
+        return -(1 + (int)er);
+    }
+    g_scenes.push_back(s);
+    return (int)g_scenes.size() - 1;
+}
+
+int sjref_n_roots(int h) {
+    if (h < 0 || h >= (int)g_scenes.size() || !g_scenes[h]) return -1;
+    return (int)g_scenes[h]->get_roots().size();
+}
+
+// Postfix program of root r; returns its node count (nothing is written when
+// it exceeds cap), -1 for a bad handle or root.
+int sjref_flatten(int h, int r, sj_csg_node* out, int cap) {
+    composite_object* root = root_of(h, r);
+    if (!root) return -1;
+    std::vector<sj_csg_node> prog;
+    flatten(root, CGS_COMPOSITE, mat3x3::id(), prog);
+    if ((int)prog.size() <= cap) memcpy(out, prog.data(), prog.size() * sizeof(sj_csg_node));
+    return (int)prog.size();
+}
+
+// The root's "eps" metadata, or def when it has none.
+double sjref_root_eps(int h, int r, double def) {
+    composite_object* root = root_of(h, r);
+    if (!root || !root->has_metadata("eps")) return def;
+    return root->fetch_metadata("eps").to_float();
+}
+
+// Susceptibilities of root r (restating parse_susceptibilities): returns the
+// count (entries beyond cap are not written) or a negative parse error.
+int sjref_root_poles(int h, int r, double* omega_0, double* gamma, double* sigma, int* drude, int cap) {
+    composite_object* root = root_of(h, r);
+    if (!root) return -1;
+    if (!root->has_metadata("susceptibilities")) return 0;
+    value val = root->fetch_metadata("susceptibilities");
+    if (val.type != VAL_LIST) return 0;
+    int n = 0;
+    for (size_t i = 0; i < val.n_els; ++i) {
+        value cur = val.val.l[i];
+        if (cur.type != VAL_LIST || cur.n_els < 3) return -2;
+        if (cur.val.l[0].type != VAL_NUM || cur.val.l[1].type != VAL_NUM || cur.val.l[2].type != VAL_NUM) return -3;
+        int use_denom = 1;
+        if (cur.n_els > 3) {
+            const value& k = cur.val.l[3];
+            if (k.type == VAL_NUM) {
+                use_denom = k.val.x != 0.0;
+            } else if (k.type == VAL_STR) {
+                if (strcmp(k.val.s, "drude") == 0 || strcmp(k.val.s, "true") == 0) use_denom = 0;
+                if (strcmp(k.val.s, "lorentz") == 0 || strcmp(k.val.s, "false") == 0) use_denom = 1;
+            } else {
+                return -3;
+            }
+        }
+        if (n < cap) {
+            omega_0[n] = cur.val.l[0].val.x;
+            gamma[n] = cur.val.l[1].val.x;
+            sigma[n] = cur.val.l[2].val.x;
+            drude[n] = !use_denom;
+        }
+        ++n;
+    }
+    return n;
+}
+
+// composite_object::in of root r at n points (xyz interleaved).
+int sjref_in(int h, int r, const double* pts, int64_t n, uint8_t* out) {
+    composite_object* root = root_of(h, r);
+    if (!root) return -1;
+    for (int64_t q = 0; q < n; ++q) out[q] = (uint8_t)root->in(vec3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]));
+    return 0;
+}
+
+}  // extern "C"

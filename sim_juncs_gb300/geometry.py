@@ -201,9 +201,22 @@ def _emit(obj, acc, out):
         raise TypeError(f"not a CSG object: {obj!r}")
 
 
+class Program(Obj):
+    """A postfix program given node by node: what a caller that flattens the
+    reference's own composite_object trees (the integration walk) passes.
+    Nodes are sj_csg_node structures or dicts with the same fields."""
+
+    def __init__(self, nodes):
+        self.nodes = [n if isinstance(n, _abi.CsgNode)
+                      else _node(n["op"], n["invert"], n["m"], n["t"], n["c"], n["p"]) for n in nodes]
+
+    def program(self):
+        return list(self.nodes)
+
+
 def as_program(obj):
     """Postfix program of any object (a bare primitive becomes a one-node program)."""
-    if isinstance(obj, Composite):
+    if isinstance(obj, (Composite, Program)):
         return obj.program()
     out = []
     _emit(obj, IDENTITY, out)

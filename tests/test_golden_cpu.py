@@ -1,0 +1,145 @@
+"""The oracle against golden vectors recorded from the reference's own code.
+
+tests/golden/cgs_reference.json comes from tests/golden/make_golden.py,
+which runs the reference's CGS parser and composite_object::in (compiled
+unmodified, oracle/_ref) on its tests/*.geom and junctions/*/junc.geom
+files.  These tests pin the oracle's CSG evaluation and rasteriser, the
+eps sum of in_bound and the susceptibility mapping to those answers, and
+check the literal values the reference's own tests assert
+(src/main_test.cpp).  The device rasteriser is checked against the same
+vectors in test_gpu_golden.py.
+"""
+import base64
+import json
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from sim_juncs_gb300 import _abi
+from sim_juncs_gb300.configs import gaussian_pulse
+from sim_juncs_gb300.geometry import Program
+from sim_juncs_gb300.spec import Grid, Region, Scene, Source, Susceptibility, scene_to_c
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "cgs_reference.json")
+
+
+def golden():
+    with open(GOLDEN) as fh:
+        return json.load(fh)
+
+
+G = golden()
+ROOTS = [(name, r) for name, e in sorted(G["files"].items()) for r in range(len(e["roots"]))]
+
+
+def unpack(bits, n):
+    return np.unpackbits(np.frombuffer(zlib.decompress(base64.b64decode(bits)), dtype=np.uint8))[:n]
+
+
+def yee_points(origin, dx, n):
+    """E-component sample points of an n^3 grid, ordered [c][k][j][i] (the
+    generator's and the rasteriser's order)."""
+    idx = np.arange(n, dtype=np.float64)
+    pts = []
+    for c in range(3):
+        ax = [origin[a] + (idx + (0.5 if c == a else 0.0)) * dx for a in range(3)]
+        z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        pts.append(np.stack([x, y, z], axis=-1).reshape(-1, 3))
+    return np.concatenate(pts)
+
+
+def golden_grid(entry):
+    g = entry["grid"]
+    return Grid(g["n"], g["n"], g["n"], g["dx"], origin=tuple(g["origin"]))
+
+
+def golden_scene(entry):
+    return Scene([Region(Program(r["nodes"]), eps=r["eps"]) for r in entry["roots"]],
+                 ambient_eps=entry["ambient_eps"])
+
+
+def test_golden_covers_the_reference_files():
+    names = set(G["files"])
+    assert "tests/test.geom" in names
+    assert "junctions/Au_SiO2_box/junc.geom" in names
+    assert "junctions/Au_SiO2_bowtie/junc.geom" in names
+    # the box junction: two roots (Au pair, SiO2 substrate), both non-empty on the grid
+    box = G["files"]["junctions/Au_SiO2_box/junc.geom"]["roots"]
+    assert len(box) == 2 and all(r["n_inside"] > 0 for r in box)
+
+
+@pytest.mark.parametrize("name,root", ROOTS)
+def test_oracle_csg_matches_reference_in(name, root):
+    e = G["files"][name]
+    g = e["grid"]
+    r = e["roots"][root]
+    pts = yee_points(g["origin"], g["dx"], g["n"])
+    want = unpack(r["inside_bits"], len(pts))
+    got = oracle.csg_in(Program(r["nodes"]).program(), pts)
+    assert int(want.sum()) == r["n_inside"]
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("name", sorted(G["files"]))
+def test_oracle_rasterizer_matches_reference_in(name):
+    e = G["files"][name]
+    n = e["grid"]["n"]
+    masks = oracle.rasterize(golden_grid(e), golden_scene(e))
+    for r, root in enumerate(e["roots"]):
+        want = unpack(root["inside_bits"], 3 * n ** 3).reshape(3, n, n, n)
+        np.testing.assert_array_equal((masks >> r) & 1, want)
+
+
+def test_reference_inclusion_test_points():
+    # src/main_test.cpp:1555-1564: in() at six points of tests/test.geom
+    e = G["files"]["tests/test.geom"]
+    tp = e["test_points"]
+    assert tp["inside"] == [1, 1, 1, 0, 0, 0]
+    got = oracle.csg_in(Program(e["roots"][0]["nodes"]).program(), np.array(tp["points"]))
+    assert got.tolist() == tp["inside"]
+
+
+def test_in_bound_sum_values():
+    # src/main_test.cpp:1637-1642: in_bound = 3.5 at the first three points,
+    # 1.0 at the others; in_bound (src/disp.cpp:264-283 with smooth_n = 0)
+    # sums def + (eps_root - def) * in(r) over the roots
+    e = G["files"]["tests/test.geom"]
+    pts = np.array(e["test_points"]["points"])
+    amb = 1.0
+    val = np.zeros(len(pts))
+    for r in e["roots"]:
+        val += amb + (r["eps"] - amb) * oracle.csg_in(Program(r["nodes"]).program(), pts)
+    assert val.tolist() == [3.5, 3.5, 3.5, 1.0, 1.0, 1.0]
+
+
+def test_susceptibilities_of_test_geom():
+    # src/main_test.cpp:1767-1776 (the C++ test compares doubles, hence float())
+    poles = G["files"]["tests/test.geom"]["roots"][0]["poles"]
+    assert [(p["omega_0"], p["gamma"], p["sigma"], p["drude"]) for p in poles] == [
+        (1.0, 0.48, 68.5971845, True), (8.0, 0.816, float(452848600800781300), True)]
+    # what the builder receives for them: sj_pole {omega_0, gamma, drude} and
+    # sigma per region
+    sus = [Susceptibility(p["omega_0"], p["gamma"], p["sigma"], drude=p["drude"]) for p in poles]
+    sc, holder = scene_to_c(Scene([Region(Program(G["files"]["tests/test.geom"]["roots"][0]["nodes"]),
+                                          eps=3.5, susceptibilities=sus)]))
+    reg = sc.contents.regions[0]
+    assert reg.n_poles == 2
+    for q, p in enumerate(poles):
+        c = reg.poles[q]
+        assert (c.omega_0, c.gamma, bool(c.drude), reg.sigma[q]) == (p["omega_0"], p["gamma"], p["drude"],
+                                                                      p["sigma"])
+
+
+def test_gaussian_source_timing():
+    # src/main_test.cpp:1785-1791 (tests/test.geom): width 3, cutoff 6,
+    # start 5.2 -> end_time = start + 2 cutoff width = 41.2
+    src = gaussian_pulse(_abi.EY, 0.2, 0.4, 1 / 1.333333, fwidth=1 / 3.0, cutoff=6.0, start_time=5.2)
+    assert src.width == pytest.approx(3.0)
+    assert src.end_time == pytest.approx(41.2)
+    # src/main_test.cpp:1876-1881: frequency 1, width 2 -> omega 2 pi, fwidth 0.5
+    s2 = Source(_abi.EX, 1.0, 2.0, 0.0, 2 * 5 * 2.0, (0, 0, 0), (1, 1, 0))
+    assert 2 * np.pi * s2.frequency == pytest.approx(6.283185307)
+    assert 1 / s2.width == pytest.approx(0.5)
