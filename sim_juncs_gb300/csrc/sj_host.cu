@@ -151,6 +151,8 @@ struct sj_sim {
     int lean_zb = -1;                  // z-segment length the tile lists were built for
     void* d_tiles = nullptr;           // tile lists of all instances and classes
     std::vector<LeanTiles> ltiles;     // per instance
+    void* d_fix = nullptr;             // correction block tables (E sources, polarisations)
+    LeanFix lfix{};
     cudaStream_t side[LEAN_STREAMS] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[LEAN_STREAMS] = {};
     // bumped whenever a descriptor changes; a graph holding parameter copies
@@ -793,6 +795,20 @@ void prepare_lean(sj_sim* sim) {
     for (int q = 0; q < sim->n_inst; ++q)
         for (int c = 0; c < LEAN_CLASSES; ++c)
             sim->ltiles[q].list[c] = base + off[(size_t)q * LEAN_CLASSES + c];
+    // correction passes (independent of the tiling)
+    std::vector<int2> passes[LEAN_FIX_PASSES];
+    lean_fix_blocks<real>(dv.data(), sim->n_inst, passes);
+    std::vector<int2> fall;
+    long long foff[LEAN_FIX_PASSES];
+    for (int p = 0; p < LEAN_FIX_PASSES; ++p) {
+        foff[p] = (long long)fall.size();
+        sim->lfix.count[p] = (long long)passes[p].size();
+        fall.insert(fall.end(), passes[p].begin(), passes[p].end());
+    }
+    sim->dfree(sim->d_fix);
+    sim->d_fix = sim->upload(fall);
+    for (int p = 0; p < LEAN_FIX_PASSES; ++p)
+        sim->lfix.blk[p] = reinterpret_cast<const int2*>(sim->d_fix) + foff[p];
     sim->lean_zb = sim->l_zb;
 }
 
@@ -827,8 +843,8 @@ cudaError_t launch_one(sj_sim* sim) {
     cudaError_t e;
     if (sim->schedule == SJ_SCHED_FUSED) {
         prepare_lean<real>(sim);
-        e = launch_lean_step<real>(dv.data(), sim->ltiles.data(), sim->n_inst, sim->l_zb, 0, sim->cur, sim->d_state,
-                                   lean_streams(sim));
+        e = launch_lean_step<real>(dv.data(), d, sim->ltiles.data(), sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur,
+                                   sim->d_state, lean_streams(sim));
     } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
@@ -857,10 +873,13 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
         sim->l_zb = zb;
         prepare_lean<real>(sim);
         const LeanTiles* lt = sim->ltiles.data();
-        ck(launch_lean_step<real>(dv.data(), lt, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls), "autotune");
+        const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
+        ck(launch_lean_step<real>(dv.data(), d, lt, sim->lfix, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+           "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
-            ck(launch_lean_step<real>(dv.data(), lt, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls), "autotune");
+            ck(launch_lean_step<real>(dv.data(), d, lt, sim->lfix, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+               "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
         float ms = 0;
@@ -1259,14 +1278,21 @@ int32_t sj_launches_per_step(const sj_sim* sim) {
         // counts from the tile classification (the lists need not be on the device yet)
         std::vector<LeanTiles> lt(sim->n_inst);
         std::vector<unsigned> lists[LEAN_CLASSES];
+        std::vector<int2> passes[LEAN_FIX_PASSES];
+        LeanFix fx{};
         for (int q = 0; q < sim->n_inst; ++q) {
             const int r = sim->precision == SJ_F64 ? lean_classify(sim->h64[q], sim->l_zb, lists)
                                                    : lean_classify(sim->h32[q], sim->l_zb, lists);
             if (r != 0) return -1;
             for (int c = 0; c < LEAN_CLASSES; ++c) lt[q].count[c] = (long long)lists[c].size();
         }
-        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), sim->n_inst)
-                                        : lean_launches(sim->h32.data(), lt.data(), sim->n_inst);
+        if (sim->precision == SJ_F64)
+            lean_fix_blocks(sim->h64.data(), sim->n_inst, passes);
+        else
+            lean_fix_blocks(sim->h32.data(), sim->n_inst, passes);
+        for (int p = 0; p < LEAN_FIX_PASSES; ++p) fx.count[p] = (long long)passes[p].size();
+        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), fx, sim->n_inst)
+                                        : lean_launches(sim->h32.data(), lt.data(), fx, sim->n_inst);
     }
     if (sim->schedule == SJ_SCHED_TMA) return 1;
     int maxp = 0;

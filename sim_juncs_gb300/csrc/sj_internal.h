@@ -110,9 +110,10 @@ cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState
                               const FusedLaunch& fl, cudaStream_t s);
 // Fused (lean) schedule.  Tiles (32 x 8 columns x zb planes) fall into four
 // classes by what their footprint touches: CPML slabs of no axis (plain),
-// of one axis (slab) or of several (multi), or a source or dispersive voxel
-// (general).  Each step is one launch per instance and non-empty class; the
-// launch carries the instance descriptor as a kernel parameter.
+// of one axis (slab) or of several (multi), or an H source (general).  E
+// sources and polarisations are corrections applied after the tiles.  Each
+// step is one launch per instance and non-empty class; the launch carries
+// the instance descriptor as a kernel parameter.
 enum { LEAN_PLAIN = 0, LEAN_SLAB = 1, LEAN_MULTI = 2, LEAN_GENERAL = 3, LEAN_CLASSES = 4 };
 template <typename real>
 struct LeanTable {
@@ -130,8 +131,17 @@ struct LeanTiles {
 long long lean_items(int nx, int ny, int nz, int zb);  // tiles of one instance
 template <typename real>
 int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists);  // -1: grid too large
+// Correction passes after the tile kernels: E sources (one pass per source
+// slot), then polarisations; blk[b] = (instance, block of that instance).
+constexpr int LEAN_FIX_PASSES = SJ_MAX_SOURCES + 1;
+struct LeanFix {
+    const int2* blk[LEAN_FIX_PASSES];
+    long long count[LEAN_FIX_PASSES];
+};
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst);  // launches per step
+void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes);
+template <typename real>
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanFix& fix, int n_inst);
 // Streams of one fused step: LEAN_SETS sets of one stream per tile class,
 // forked from `main` and joined back into it with the events; instance q's
 // launches go to set q % LEAN_SETS, so the small launches of many instances
@@ -144,8 +154,9 @@ struct LeanStreams {
     cudaEvent_t fork, join[LEAN_STREAMS];
 };
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls);
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
+                             const LeanFix& fix, int n_inst, int zb, int dry, int cur, DevState* st,
+                             const LeanStreams& ls);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>

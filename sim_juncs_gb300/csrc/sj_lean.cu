@@ -28,11 +28,14 @@
 // read the step counter) count themselves, and the last one advances the
 // step.  A step launches each non-empty class of each instance on streams
 // forked from the caller's (one per class and instance set), so the kernels
-// overlap.  All
-// evaluate one update formula, so a voxel's result does not depend on which
-// kernel (or which tiling) updated it:
+// overlap; after they join, small correction kernels add the E sources and
+// the polarisation ADE on their cells only.  All evaluate one update formula,
+// so a voxel's result does not depend on which kernel (or which tiling)
+// updated it:
 //   H^{n+1/2} = fma(-S, curl E, H^{n-1/2}) [- dt J_H]
-//   E^{n+1}   = fma(S ε∞⁻¹, curl H, E^n) [then fma(-ε∞⁻¹, dt J + Σ_p ΔP_p, ·)]
+//   E^{n+1}   = fma(S ε∞⁻¹, curl H, E^n)
+//               [then fma(-ε∞⁻¹, dt J_s, ·) per E source s, in order]
+//               [then fma(-ε∞⁻¹, Σ_p (P_p^{n+1} - P_p^n), ·)]
 // with curl including the CPML ψ terms.  This file is compiled with
 // contraction off (-fmad=false): every fused multiply-add is the explicit
 // one written here.
@@ -44,6 +47,7 @@
 namespace sj {
 
 constexpr int LX = 32, LY = 8;      // tile of columns per block
+constexpr int FIX_THREADS = 256;    // cells per block of the correction kernels
 constexpr int LMAXF = 256;
 
 // resident blocks per SM each kernel is compiled for (register budget)
@@ -97,23 +101,22 @@ __device__ __forceinline__ real ldz(const real* p, long long o, bool ok) {
 __host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ inline int imin(int a, int b) { return a < b ? a : b; }
 
-// Does the tile's footprint touch a source (own cells and the x-1 / y-1 /
-// z-1 neighbours whose H it recomputes), or do its own cells touch the
-// bounding box of the dispersive voxels?  Block-uniform.
+// Does the tile's footprint (own cells and the x-1 / y-1 / z-1 neighbours
+// whose H it recomputes) touch an H source?  E sources and polarisations
+// are applied after the tile kernels (k_lean_esrc, k_lean_disp), so only H
+// sources, which the E update of the same pass reads, need the general
+// kernel.  Block-uniform.
 template <typename real>
-__host__ __device__ inline bool tile_has_extras(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
+__host__ __device__ inline bool tile_has_hsource(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
     const int xa = imax(i0 - 1, 0), xb = imin(i0 + LX, I.nx) - 1;
     const int ya = imax(j0 - 1, 0), yb = imin(j0 + LY, I.ny) - 1;
     const int za = imax(z0 - 1, 0), zb = z1 - 1;
     for (int q = 0; q < I.n_src; ++q) {
         const SrcDev<real>& sv = I.src[q];
-        if (sv.lo[0] <= xb && sv.lo[0] + sv.n[0] > xa && sv.lo[1] <= yb && sv.lo[1] + sv.n[1] > ya &&
-            sv.lo[2] <= zb && sv.lo[2] + sv.n[2] > za)
+        if (sv.comp >= 3 && sv.lo[0] <= xb && sv.lo[0] + sv.n[0] > xa && sv.lo[1] <= yb &&
+            sv.lo[1] + sv.n[1] > ya && sv.lo[2] <= zb && sv.lo[2] + sv.n[2] > za)
             return true;
     }
-    if (I.n_poles > 0 && I.dvol > 0 && I.dlo[0] <= xb && I.dlo[0] + I.dn[0] > i0 && I.dlo[1] <= yb &&
-        I.dlo[1] + I.dn[1] > j0 && I.dlo[2] <= zb && I.dlo[2] + I.dn[2] > z0)
-        return true;
     return false;
 }
 
@@ -238,33 +241,11 @@ __device__ __forceinline__ real h_new(const InstDev<real>& I, int comp, real cv,
     return h;
 }
 
-// E^{n+1} of the own cell: Yee term, then sources and the polarisation ADE
-// as one correction scaled by eps_inf^{-1}.
-template <bool EXTRAS, int CA, typename real>
-__device__ __forceinline__ real e_new(const InstDev<real>& I, int i, int j, int k, long long n, const real* cf,
-                                      bool disp, real e_old, real cv, bool store, bool src) {
-    real e = fma(I.S * ldg(cf, CA), cv, e_old);
-    if (!EXTRAS) return e;
-    bool hit = false;
-    real corr = src ? source_sum(I, CA, i, j, k, n, hit) : real(0);
-    if (disp) {
-        const long long di =
-            ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]);
-        for (int p = 0; p < I.n_poles; ++p) {
-            real* pp = I.P + ((long long)(p * 2 + 0) * 3 + CA) * I.dvol + di;
-            real* pm = I.P + ((long long)(p * 2 + 1) * 3 + CA) * I.dvol + di;
-            const real pn = *pp, pq = *pm;
-            const real pnew = I.A[p] * pn + I.B[p] * pq + ldg(cf, 3 + 3 * p + CA) * e_old;
-            corr += pnew - pn;
-            if (store) {
-                *pm = pn;
-                *pp = pnew;
-            }
-        }
-        hit = true;
-    }
-    if (hit) e = fma(-ldg(cf, CA), corr, e);
-    return e;
+// E^{n+1} of the own cell, Yee and CPML terms (sources and polarisations are
+// applied by k_lean_esrc and k_lean_disp after the tile kernels).
+template <int CA, typename real>
+__device__ __forceinline__ real e_new(const InstDev<real>& I, const real* cf, real e_old, real cv) {
+    return fma(I.S * ldg(cf, CA), cv, e_old);
 }
 
 // Slab axes a tile's footprint touches (bit a = axis a): the same footprint
@@ -279,7 +260,7 @@ __host__ __device__ inline int tile_slab_mask(const InstDev<real>& I, int i0, in
 }
 
 // Tile update with CPML on the axes in MASK (runtime per-cell flags inside)
-// and, with EXTRAS, sources and polarisations.  The x and y profile values of
+// and, with EXTRAS, H sources.  The x and y profile values of
 // the column are loaded once; z values once per plane.
 template <typename real, int ZB, int MASK, bool EXTRAS>
 __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int ty, int tz, long long n, bool dry) {
@@ -330,12 +311,13 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
         if (yo) byi = ldg(pr, j), cyi = ldg(pr, ny + j), byh = ldg(pr, 2 * ny + j), cyh = ldg(pr, 3 * ny + j);
         if (yo_m) byhm = ldg(pr, 2 * ny + j - 1), cyhm = ldg(pr, 3 * ny + j - 1);
     }
-    // sources touching this column's footprint (own, x-1 and y-1 cells)
+    // H sources touching this column's footprint (own, x-1 and y-1 cells)
     unsigned smask = 0;
     if (EXTRAS)
         for (int q = 0; q < I.n_src; ++q) {
             const SrcDev<real>& sv = I.src[q];
-            if (sv.lo[0] <= i && sv.lo[0] + sv.n[0] > i - 1 && sv.lo[1] <= j && sv.lo[1] + sv.n[1] > j - 1)
+            if (sv.comp >= 3 && sv.lo[0] <= i && sv.lo[0] + sv.n[0] > i - 1 && sv.lo[1] <= j &&
+                sv.lo[1] + sv.n[1] > j - 1)
                 smask |= 1u << q;
         }
 
@@ -463,30 +445,28 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
             oHY[o] = hy;
             oHZ[o] = hz;
             // E^{n+1} at the own cell
-            const int cb = __ldg(I.combo + o);
-            const real* cf = I.coef + cb * I.ncoef;
-            const bool disp = EXTRAS && (__ldg(I.cflag + cb) & 1) != 0;
+            const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
             const bool si = !dry;
             {
                 const real d1 = hz - hz_ym, d2 = hy - hyp;
                 real cv = d1 - d2;
                 pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
                 pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
-                oEX[o] = e_new<EXTRAS, 0>(I, i, j, k, n, cf, disp, ex_c, cv, si, src);
+                oEX[o] = e_new<0>(I, cf, ex_c, cv);
             }
             {
                 const real d1 = hx - hxp, d2 = hz - hz_xm;
                 real cv = d1 - d2;
                 pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
                 pml_term<SX, false, false>(cv, xo, bxi, cxi, d2, peX, peX, o, si);
-                oEY[o] = e_new<EXTRAS, 1>(I, i, j, k, n, cf, disp, ey_c, cv, si, src);
+                oEY[o] = e_new<1>(I, cf, ey_c, cv);
             }
             {
                 const real d1 = hy - hy_xm, d2 = hx - hx_ym;
                 real cv = d1 - d2;
                 pml_term<SX, true, false>(cv, xo, bxi, cxi, d1, peX + vol, peX + vol, o, si);
                 pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
-                oEZ[o] = e_new<EXTRAS, 2>(I, i, j, k, n, cf, disp, ez, cv, si, src);
+                oEZ[o] = e_new<2>(I, cf, ez, cv);
             }
         }
         hxp = hx;
@@ -561,17 +541,17 @@ __device__ __forceinline__ void tile_decode(unsigned code, int& tx, int& ty, int
     mask = (int)(code >> 29);
 }
 
-// Only the general launches read the step counter (sources, probes): their
-// blocks count themselves, and the last one of the step advances the step
-// and flips the device copy of the parity.
-template <typename real>
-__device__ __forceinline__ void finish_block(const LeanTable<real>& tab, DevState* st) {
+// Only the general and correction launches read the step counter (sources,
+// probes): their blocks count themselves, and the last one of the step
+// (step_blocks in all) advances the step and flips the device copy of the
+// parity.
+__device__ __forceinline__ void finish_block(unsigned step_blocks, int dry, DevState* st) {
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         __threadfence();
         const unsigned prev = atomicAdd(&st->done, 1u);
-        if (prev == tab.step_blocks - 1) {
-            if (!tab.dry) {
+        if (prev == step_blocks - 1) {
+            if (!dry) {
                 st->step += 1;
                 st->cur ^= 1;
             }
@@ -636,7 +616,77 @@ k_lean_general(const __grid_constant__ LeanTable<real> tab, DevState* st) {
     } else if (!tab.dry) {
         lean_probe_block<real>(tab.inst, b - tab.n_tiles, n, 0, st);
     }
-    finish_block(tab, st);
+    finish_block(tab.step_blocks, tab.dry, st);
+}
+
+// ------------------------------------------------------------ corrections
+// After the tile kernels of a step, on the caller's stream and in this
+// order: one k_lean_esrc launch per source slot s (the instances whose
+// source s is an E source), then one k_lean_disp launch (the instances with
+// dispersive voxels).  Block b takes FIX_THREADS cells of one instance's box:
+// blk[b] = (instance, first cell / FIX_THREADS).  Descriptors come from the
+// device table; `cur` is the step's parity.
+
+// E^{n+1} = fma(-eps_inf^{-1}, dt J_s, E^{n+1}) over source s's box
+template <typename real>
+__global__ void __launch_bounds__(FIX_THREADS)
+k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int slot, int cur,
+            unsigned step_blocks, int dry, DevState* st) {
+    const long long n = st->step;
+    const int2 e = __ldg(blk + blockIdx.x);
+    const InstDev<real>& I = insts[e.x];
+    const SrcDev<real>& sv = I.src[slot];
+    const long long cell = (long long)e.y * FIX_THREADS + threadIdx.x;
+    const long long n01 = (long long)sv.n[0] * sv.n[1];
+    if (cell < n01 * sv.n[2]) {
+        const int di = (int)(cell % sv.n[0]), dj = (int)((cell / sv.n[0]) % sv.n[1]), dk = (int)(cell / n01);
+        const long long o = (long long)(sv.lo[2] + dk) * I.plane + (long long)(sv.lo[1] + dj) * I.px + (sv.lo[0] + di);
+        real* E = I.F[cur ^ 1][sv.comp];
+        const real cfc = I.coef[(int)I.combo[o] * I.ncoef + sv.comp];
+        const real J = (real)sv.tab[n] * sv.w[0][di] * sv.w[1][dj] * sv.w[2][dk];
+        E[o] = fma(-cfc, J, E[o]);
+    }
+    finish_block(step_blocks, dry, st);
+}
+
+// meep's Lorentz/Drude ADE over the dispersive bounding box:
+// P^{n+1} = A P^n + B P^{n-1} + C sigma E^n per pole, and
+// E^{n+1} = fma(-eps_inf^{-1}, sum_p (P^{n+1} - P^n), E^{n+1})
+template <typename real>
+__global__ void __launch_bounds__(FIX_THREADS)
+k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int cur, unsigned step_blocks,
+            int dry, DevState* st) {
+    const int2 e = __ldg(blk + blockIdx.x);
+    const InstDev<real>& I = insts[e.x];
+    const long long di = (long long)e.y * FIX_THREADS + threadIdx.x;
+    if (di < I.dvol) {
+        const int i = I.dlo[0] + (int)(di % I.dn[0]);
+        const int j = I.dlo[1] + (int)((di / I.dn[0]) % I.dn[1]);
+        const int k = I.dlo[2] + (int)(di / ((long long)I.dn[0] * I.dn[1]));
+        const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+        const int cb = I.combo[o];
+        if (I.cflag[cb] & 1) {
+            const real* cf = I.coef + cb * I.ncoef;
+            for (int c = 0; c < 3; ++c) {
+                const real e_old = I.F[cur][c][o];
+                real corr = 0;
+                for (int p = 0; p < I.n_poles; ++p) {
+                    real* pp = I.P + ((long long)(p * 2 + 0) * 3 + c) * I.dvol + di;
+                    real* pm = I.P + ((long long)(p * 2 + 1) * 3 + c) * I.dvol + di;
+                    const real pn = *pp, pq = *pm;
+                    const real pnew = I.A[p] * pn + I.B[p] * pq + cf[3 + 3 * p + c] * e_old;
+                    corr += pnew - pn;
+                    if (!dry) {
+                        *pm = pn;
+                        *pp = pnew;
+                    }
+                }
+                real* E = I.F[cur ^ 1][c];
+                E[o] = fma(-cf[c], corr, E[o]);
+            }
+        }
+    }
+    finish_block(step_blocks, dry, st);
 }
 
 long long lean_items(int nx, int ny, int nz, int zb) {
@@ -653,7 +703,7 @@ int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists) 
             for (int tx = 0; tx < ntx; ++tx) {
                 const int i0 = tx * LX, j0 = ty * LY, z0 = tz * zb, z1 = imin(I.nz, z0 + zb);
                 const int m = tile_slab_mask(I, i0, j0, z0, z1);
-                const int c = tile_has_extras(I, i0, j0, z0, z1) ? LEAN_GENERAL
+                const int c = tile_has_hsource(I, i0, j0, z0, z1) ? LEAN_GENERAL
                               : m == 0                           ? LEAN_PLAIN
                               : (m == 1 || m == 2 || m == 4)     ? LEAN_SLAB
                                                                  : LEAN_MULTI;
@@ -682,8 +732,9 @@ long long general_blocks(const InstDev<real>& I, const LeanTiles& T, int q, int 
 }  // namespace
 
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst) {
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanFix& fix, int n_inst) {
     int total = 0;
+    for (int p = 0; p < LEAN_FIX_PASSES; ++p) total += fix.count[p] > 0;
     for (int q = 0; q < n_inst; ++q) {
         for (int c = 0; c < LEAN_CLASSES; ++c)
             if (c != LEAN_GENERAL && tiles[q].count[c] > 0) ++total;
@@ -691,15 +742,34 @@ int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_in
     }
     return total;
 }
-template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, int);
-template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, int);
+template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, const LeanFix&, int);
+template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, const LeanFix&, int);
+
+template <typename real>
+void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes) {
+    for (int p = 0; p < LEAN_FIX_PASSES; ++p) passes[p].clear();
+    for (int q = 0; q < n_inst; ++q) {
+        const InstDev<real>& I = h_insts[q];
+        for (int s = 0; s < I.n_src; ++s) {
+            if (I.src[s].comp >= 3) continue;
+            const long long cells = (long long)I.src[s].n[0] * I.src[s].n[1] * I.src[s].n[2];
+            for (long long b = 0; b * FIX_THREADS < cells; ++b) passes[s].push_back(make_int2(q, (int)b));
+        }
+        if (I.n_poles > 0 && I.dvol > 0)
+            for (long long b = 0; b * FIX_THREADS < I.dvol; ++b)
+                passes[SJ_MAX_SOURCES].push_back(make_int2(q, (int)b));
+    }
+}
+template void lean_fix_blocks<float>(const InstDev<float>*, int, std::vector<int2>*);
+template void lean_fix_blocks<double>(const InstDev<double>*, int, std::vector<int2>*);
 
 // Each class of instance q goes to its own stream of set q % LEAN_SETS: the
 // kernels of a step overlap and fill each other's tails.  Only as many sets
 // as there are instances are forked.
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tiles, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls) {
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
+                             const LeanFix& fix, int n_inst, int zb, int dry, int cur, DevState* st,
+                             const LeanStreams& ls) {
     cudaError_t e = cudaSuccess;
     const bool fork = ls.side[0] != nullptr;
     const int nsets = fork ? std::min(n_inst, LEAN_SETS) : 0;
@@ -711,6 +781,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tile
     }
     long long gtotal = 0;
     for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
+    for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
     const dim3 block(LX, LY);
     for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
         LeanTable<real> t;
@@ -753,11 +824,20 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const LeanTiles* tile
             if (e == cudaSuccess) e = cudaStreamWaitEvent(ls.main, ls.join[q], 0);
         }
     }
+    for (int p = 0; p < LEAN_FIX_PASSES && e == cudaSuccess; ++p) {
+        if (!fix.count[p]) continue;
+        const unsigned nb = (unsigned)fix.count[p];
+        if (p < SJ_MAX_SOURCES)
+            k_lean_esrc<real><<<nb, FIX_THREADS, 0, ls.main>>>(d_insts, fix.blk[p], p, cur, (unsigned)gtotal, dry, st);
+        else
+            k_lean_disp<real><<<nb, FIX_THREADS, 0, ls.main>>>(d_insts, fix.blk[p], cur, (unsigned)gtotal, dry, st);
+        e = cudaGetLastError();
+    }
     return e;
 }
 
-template cudaError_t launch_lean_step<double>(const InstDev<double>*, const LeanTiles*, int, int, int, int, DevState*,
-                                              const LeanStreams&);
-template cudaError_t launch_lean_step<float>(const InstDev<float>*, const LeanTiles*, int, int, int, int, DevState*,
-                                             const LeanStreams&);
+template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*, const LeanTiles*,
+                                              const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
+template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const LeanTiles*,
+                                             const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
 }  // namespace sj

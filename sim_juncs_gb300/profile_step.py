@@ -1,0 +1,48 @@
+"""Run a few steps of a named workload, for profilers (ncu) to capture.
+
+    python -m sim_juncs_gb300.profile_step WORKLOAD [--precision f32|f64]
+        [--schedule fused|tma|split] [--zseg Z] [--steps N]
+
+Workloads: sweep (32 x 96^3 + 32 x 128^3 + 32 x 192^3 junctions),
+junction192 (one 192^3 sweep member), bowtie (512 x 512 x 384),
+junction64 (64^3).  Prints the launches per step so that a capture can
+skip set-up launches and warm-up steps by count.
+"""
+import argparse
+
+from . import configs
+from .fields import Fields
+
+
+def instances(name):
+    if name == "sweep":
+        return configs.sweep_instances()
+    if name == "junction192":
+        return [configs.junction_instance(n=192, res=60.0, probe_components=("Ez",), dft=False)]
+    if name == "bowtie":
+        return [configs.bowtie_instance()]
+    if name == "junction64":
+        return [configs.junction_instance()]
+    raise SystemExit(f"unknown workload {name!r}")
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("workload")
+    p.add_argument("--precision", default="f32")
+    p.add_argument("--schedule", default=None)
+    p.add_argument("--zseg", type=int, default=8)
+    p.add_argument("--steps", type=int, default=3)
+    a = p.parse_args()
+    f = Fields(instances(a.workload), a.precision, a.schedule)
+    if f.schedule_name() == "fused":
+        f.set_tiling(8, 0, a.zseg)
+    f.step(a.steps)
+    f.synchronize()
+    print(f"{a.workload} {a.precision} {f.schedule_name()} steps={f.steps_done} voxels={f.voxels()} "
+          f"launches_per_step={f.launches_per_step()}", flush=True)
+    f.close()
+
+
+if __name__ == "__main__":
+    main()
