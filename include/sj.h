@@ -261,7 +261,7 @@ int32_t sj_get_schedule(const sj_sim* sim);
 int sj_synchronize(sj_sim* sim);
 
 /* tiling of the single-pass schedules.  FUSED: blocks of 32 x 8 columns
-   march z segments of zseg in {8, 16, 32, 64} planes (tile_y, ring ignored).
+   march z segments of zseg in {8, 16, 32} planes (tile_y, ring ignored).
    TMA: tiles of 32 x tile_y cells, a TMA ring of `ring` planes
    ((tile_y, ring) in {(4,3), (8,3), (16,3), (4,4), (8,4)}), z segments of
    zseg planes.  Applies to the schedule selected when it is called. */

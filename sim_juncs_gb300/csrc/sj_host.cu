@@ -781,6 +781,8 @@ void prepare_lean(sj_sim* sim) {
     std::vector<unsigned> lists[LEAN_CLASSES];
     sim->ltiles.assign(sim->n_inst, LeanTiles{});
     for (int q = 0; q < sim->n_inst; ++q) {
+        if (2 * dv[q].vol >= (1LL << 32))
+            fail(SJ_E_INVALID, "grid too large for the fused schedule's 32-bit offsets (use split or tma)");
         if (lean_classify<real>(dv[q], sim->l_zb, lists) != 0)
             fail(SJ_E_INVALID, "grid too large for the fused schedule's tile codes");
         for (int c = 0; c < LEAN_CLASSES; ++c) {
@@ -860,7 +862,7 @@ cudaError_t launch_one(sj_sim* sim) {
 // Lean-schedule autotuner: z-segment length by timing dry launches.
 template <typename real>
 void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
-    const int zbs[4] = {8, 16, 32, 64};
+    const int zbs[3] = {8, 16, 32};
     float best = 1e30f;
     int bzb = sim->l_zb;
     cudaEvent_t e0, e1;
@@ -1175,8 +1177,8 @@ int sj_set_schedule(sj_sim* sim, int32_t schedule) {
 int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {
     if (!sim) return SJ_E_INVALID;
     if (sim->schedule == SJ_SCHED_FUSED) {
-        if (zseg != 8 && zseg != 16 && zseg != 32 && zseg != 64)
-            return finish(sim, SJ_E_INVALID, "fused schedule: zseg must be 8, 16, 32 or 64");
+        if (zseg != 8 && zseg != 16 && zseg != 32)
+            return finish(sim, SJ_E_INVALID, "fused schedule: zseg must be 8, 16 or 32");
         sim->l_zb = zseg;
         sim->drop_graphs();
         return SJ_OK;

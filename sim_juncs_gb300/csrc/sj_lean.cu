@@ -52,16 +52,16 @@ constexpr int LMAXF = 256;
 
 // resident blocks per SM each kernel is compiled for (register budget)
 #ifndef SJ_LEAN_PLAIN_MINB
-#define SJ_LEAN_PLAIN_MINB 4
+#define SJ_LEAN_PLAIN_MINB 5
 #endif
 #ifndef SJ_LEAN_SLAB_MINB
-#define SJ_LEAN_SLAB_MINB 4
+#define SJ_LEAN_SLAB_MINB 5
 #endif
 #ifndef SJ_LEAN_MULTI_MINB
-#define SJ_LEAN_MULTI_MINB 3
+#define SJ_LEAN_MULTI_MINB 4
 #endif
 #ifndef SJ_LEAN_GEN_MINB
-#define SJ_LEAN_GEN_MINB 3
+#define SJ_LEAN_GEN_MINB 4
 #endif
 template <typename real>
 constexpr int plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PLAIN_MINB : 3; }
@@ -89,12 +89,15 @@ __device__ __forceinline__ void prefetch_row(const T* p) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "n"(32 * sizeof(T)));
 }
 
+// Element offsets within an instance are 32-bit (the host rejects grids
+// whose two-slot psi arrays would not fit): one wide multiply-add per
+// address.
 template <typename real>
-__device__ __forceinline__ real ldg(const real* p, long long o) {
+__device__ __forceinline__ real ldg(const real* p, unsigned o) {
     return __ldg(p + o);
 }
 template <typename real>
-__device__ __forceinline__ real ldz(const real* p, long long o, bool ok) {
+__device__ __forceinline__ real ldz(const real* p, unsigned o, bool ok) {
     return ok ? __ldg(p + o) : real(0);
 }
 
@@ -121,12 +124,14 @@ __host__ __device__ inline bool tile_has_hsource(const InstDev<real>& I, int i0,
 }
 
 // ------------------------------------------------------------- plain tiles
-template <typename real, int ZB>
+// EDGE = false: the tile's footprint and its z+1 plane stay inside the grid,
+// so no load needs a bounds predicate.
+template <typename real, int ZB, bool EDGE>
 __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int ty, int tz) {
     const int i = tx * LX + threadIdx.x, j = ty * LY + threadIdx.y;
     const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
-    if (i >= I.nx || j >= I.ny) return;
-    const long long px = I.px, plane = I.plane;
+    if (EDGE && (i >= I.nx || j >= I.ny)) return;
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane;
     const real* eX = I.F[0][0];
     const real* eY = I.F[0][1];
     const real* eZ = I.F[0][2];
@@ -140,18 +145,18 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
     real* oHY = I.F[1][4];
     real* oHZ = I.F[1][5];
     const real S = I.S;
-    const bool xm = i > 0, ym = j > 0, xp = i + 1 < I.nx, yp = j + 1 < I.ny;
+    const bool xm = !EDGE || i > 0, ym = !EDGE || j > 0, xp = !EDGE || i + 1 < I.nx, yp = !EDGE || j + 1 < I.ny;
 
     int k = z0 > 0 ? z0 - 1 : 0;
-    long long o = (long long)k * plane + (long long)j * px + i;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;
-    const long long orow = o - threadIdx.x;  // row start of this warp at plane k
+    const unsigned orow = o - threadIdx.x;  // row start of this warp at plane k
     for (; k < z1; ++k, o += plane) {
-        const bool kp = k + 1 < I.nz;
+        const bool kp = !EDGE || k + 1 < I.nz;
         if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < I.nz && k + LEAN_PF < z1) {
-            const long long r = orow + (long long)(k - (z0 > 0 ? z0 - 1 : 0) + 1 + LEAN_PF) * plane;
+            const unsigned r = orow + (unsigned)(k - (z0 > 0 ? z0 - 1 : 0) + 1 + LEAN_PF) * plane;
             prefetch_row(eX + r);
             prefetch_row(eY + r);
             prefetch_row(eZ + r);
@@ -218,7 +223,7 @@ __device__ __forceinline__ real source_sum(const InstDev<real>& I, int comp, int
 // (compile time) removes axes a tile cannot touch.
 template <bool AX, bool ADD, bool NC, typename real>
 __device__ __forceinline__ void pml_term(real& cv, bool on, real b, real c, real d, const real* pin, real* pout,
-                                         long long x, bool store) {
+                                         unsigned x, bool store) {
     if (!AX) return;
     const real po = on ? (NC ? __ldg(pin + x) : pin[x]) : real(0);
     const real ps = fma(b, po, c * d);
@@ -262,15 +267,15 @@ __host__ __device__ inline int tile_slab_mask(const InstDev<real>& I, int i0, in
 // Tile update with CPML on the axes in MASK (runtime per-cell flags inside)
 // and, with EXTRAS, H sources.  The x and y profile values of
 // the column are loaded once; z values once per plane.
-template <typename real, int ZB, int MASK, bool EXTRAS>
+template <typename real, int ZB, int MASK, bool EXTRAS, bool EDGE>
 __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int ty, int tz, long long n, bool dry) {
     constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
     const int i = tx * LX + threadIdx.x, j = ty * LY + threadIdx.y;
     const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
-    if (i >= I.nx || j >= I.ny) return;
+    if (EDGE && (i >= I.nx || j >= I.ny)) return;
 
     const int nx = I.nx, ny = I.ny, nz = I.nz;
-    const long long px = I.px, plane = I.plane, vol = I.vol;
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
     const real* eX = I.F[0][0];
     const real* eY = I.F[0][1];
     const real* eZ = I.F[0][2];
@@ -294,7 +299,7 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
     real* peY = SY ? I.psiE[1] : nullptr;
     real* peZ = SZ ? I.psiE[2] : nullptr;
 
-    const bool xm = i > 0, ym = j > 0, xp = i + 1 < nx, yp = j + 1 < ny;
+    const bool xm = !EDGE || i > 0, ym = !EDGE || j > 0, xp = !EDGE || i + 1 < nx, yp = !EDGE || j + 1 < ny;
     // CPML slab membership of the own cell and of the two recomputed neighbours
     const bool xo = SX && in_slab(I, 0, i), xo_m = SX && xm && in_slab(I, 0, i - 1);
     const bool yo = SY && in_slab(I, 1, j), yo_m = SY && ym && in_slab(I, 1, j - 1);
@@ -322,24 +327,24 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
         }
 
     int k = z0 > 0 ? z0 - 1 : 0;
-    long long o = (long long)k * plane + (long long)j * px + i;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
     // E^n of plane k carried between iterations: own Ex, Ey; Ex at (i-1); Ey at (j-1)
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;  // H^{n+1/2} of plane k-1 at the own cell
-    const long long orow = o - threadIdx.x;  // row start of this warp at plane k
+    const unsigned orow = o - threadIdx.x;  // row start of this warp at plane k
     const int k0 = k;
     // the x psi rows are prefetched only where the tile touches an x slab
     // (the arrays exist only for axes with slabs)
     const int i0 = tx * LX;
     const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
     for (; k < z1; ++k, o += plane) {
-        const bool kp = k + 1 < nz;
+        const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
         if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < nz && k + LEAN_PF < z1) {
             const int kq = k + 1 + LEAN_PF;
-            const long long r = orow + (long long)(kq - k0) * plane;
+            const unsigned r = orow + (unsigned)(kq - k0) * plane;
             prefetch_row(eX + r);
             prefetch_row(eY + r);
             prefetch_row(eZ + r);
@@ -408,7 +413,7 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
             // ... and, recomputed (psi read only), at (i-1, j) [Hy, Hz] and (i, j-1) [Hx, Hz]
             real hy_xm = 0, hz_xm = 0, hx_ym = 0, hz_ym = 0;
             if (xm) {
-                const long long om = o - 1;
+                const unsigned om = o - 1;
                 {
                     const real d1 = exm_n - exm_c, d2 = ez - ez_xm;
                     real cv = d1 - d2;
@@ -425,7 +430,7 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
                 }
             }
             if (ym) {
-                const long long om = o - px;
+                const unsigned om = o - px;
                 {
                     const real d1 = ez - ez_ym, d2 = eym_n - eym_c;
                     real cv = d1 - d2;
@@ -562,12 +567,31 @@ __device__ __forceinline__ void finish_block(unsigned step_blocks, int dry, DevS
 }
 
 // Plain tiles: no CPML slab, source or dispersive voxel in the footprint.
+// Does the tile's footprint or its z+1 plane reach a face of the grid?
+template <typename real>
+__device__ __forceinline__ bool tile_edge(const InstDev<real>& I, int tx, int ty, int tz, int zb) {
+    const int i0 = tx * LX, j0 = ty * LY, z1 = min(I.nz, (tz + 1) * zb);
+    return !(i0 > 0 && i0 + LX < I.nx && j0 > 0 && j0 + LY < I.ny && z1 < I.nz);
+}
+
 template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, plain_minb<real>())
 k_lean_plain(const __grid_constant__ LeanTable<real> tab) {
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
-    plain_block<real, ZB>(tab.inst, tx, ty, tz);
+    if (tile_edge(tab.inst, tx, ty, tz, ZB))
+        plain_block<real, ZB, true>(tab.inst, tx, ty, tz);
+    else
+        plain_block<real, ZB, false>(tab.inst, tx, ty, tz);
+}
+
+template <typename real, int ZB, int MASK, bool EXTRAS>
+__device__ __forceinline__ void tile_block_any(const InstDev<real>& I, int tx, int ty, int tz, long long n,
+                                               bool dry) {
+    if (tile_edge(I, tx, ty, tz, ZB))
+        tile_block<real, ZB, MASK, EXTRAS, true>(I, tx, ty, tz, n, dry);
+    else
+        tile_block<real, ZB, MASK, EXTRAS, false>(I, tx, ty, tz, n, dry);
 }
 
 // Single-slab tiles: the footprint touches the slabs of exactly one axis.
@@ -577,11 +601,11 @@ k_lean_slab(const __grid_constant__ LeanTable<real> tab) {
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     if (m == 1)
-        tile_block<real, ZB, 1, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 1, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else if (m == 2)
-        tile_block<real, ZB, 2, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 2, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else
-        tile_block<real, ZB, 4, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 4, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
 }
 
 // Multi-slab tiles: the slabs of two or three axes (edges and corners).
@@ -591,13 +615,13 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     if (m == 3)
-        tile_block<real, ZB, 3, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 3, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else if (m == 5)
-        tile_block<real, ZB, 5, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 5, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else if (m == 6)
-        tile_block<real, ZB, 6, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 6, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else
-        tile_block<real, ZB, 7, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_block_any<real, ZB, 7, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
 }
 
 // General tiles (a source or dispersive voxel in the footprint), then the
@@ -612,7 +636,7 @@ k_lean_general(const __grid_constant__ LeanTable<real> tab, DevState* st) {
         tile_decode(__ldg(tab.tiles + b), tx, ty, tz, m);
         // tile_block returns early for columns outside the grid; every
         // thread still reaches the barrier in finish_block
-        tile_block<real, ZB, 7, true>(tab.inst, tx, ty, tz, n, tab.dry != 0);
+        tile_block<real, ZB, 7, true, true>(tab.inst, tx, ty, tz, n, tab.dry != 0);
     } else if (!tab.dry) {
         lean_probe_block<real>(tab.inst, b - tab.n_tiles, n, 0, st);
     }
@@ -812,7 +836,6 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
             SJ_ZB(8)
             SJ_ZB(16)
             SJ_ZB(32)
-            SJ_ZB(64)
             default: return cudaErrorInvalidValue;
         }
 #undef SJ_ZB

@@ -156,12 +156,12 @@ def test_tma_tilings_agree(lib, ty, ring, zs):
     np.testing.assert_array_equal(b.monitors(), a.monitors())
 
 
-@pytest.mark.parametrize("zs", [8, 32, 64])
+@pytest.mark.parametrize("zs", [8, 32])
 def test_fused_zsegments_agree(lib, zs):
     # the z-segment length moves tiles between the plain and the general
     # kernel; both evaluate the same formula, so the bits do not change
     inst = junction_instance(n=96, res=30.0)
-    assert plain_tiles(inst, 16) > 0          # zs = 64 leaves none: all general
+    assert plain_tiles(inst, 16) > 0
     a = Fields(inst, "f32", "fused")
     b = Fields(inst, "f32", "fused")
     a.set_tiling(8, 0, 16)
@@ -210,7 +210,7 @@ def test_autotune_leaves_state_untouched(lib, schedule):
     b.step(50)
     ty, ring, zs, ms = b.autotune(steps=2)
     if schedule == "fused":
-        assert (ty, ring) == (8, 0) and zs in (8, 16, 32, 64) and ms > 0
+        assert (ty, ring) == (8, 0) and zs in (8, 16, 32) and ms > 0
     else:
         assert ty in (4, 8, 16) and ring in (3, 4) and zs >= 1 and ms > 0
     assert b.steps_done == 50
