@@ -315,6 +315,50 @@ int sj_read_class_map(sj_sim* sim, int32_t inst, uint8_t* out, size_t cap);
 /* largest |E| over the instance (divergence guard, src/disp.cpp:727-729) */
 int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out);
 
+/* ---------------------------------------------------------------- adjoint */
+/* Gradient of a gap-field objective with respect to per-voxel eps (the
+   adjoint item of the replacement interface; the reference has no
+   counterpart).
+
+   Design region: a box of voxels whose eps_inf is given per voxel and
+   applies at the voxel's Ex, Ey and Ez points (replacing the class table's
+   value there; polarisations of the voxel's class still apply).  An
+   instance with a design region steps with the split schedule.
+
+   Objective: F = sum over cells and over the E components in comp_mask of
+   |D_c|^2 with D_c = sum_{n=0}^{N-1} dt E_c^n(cell) e^{+i 2 pi f n dt}, the
+   running DFT of E sampled before each of the N steps (the probes'
+   convention).
+
+   sj_adjoint_gradient restarts every instance from zero fields at t = 0,
+   runs N steps forward keeping the full state every checkpoint_every steps,
+   then runs the discrete adjoint of the stepper backwards (the exact
+   transpose of each sub-update: H and its CPML psi, E and its psi, the
+   polarisation ADE), re-running each segment forward from its checkpoint
+   to regenerate what the gradient needs.  d_obj_d_eps receives, instance
+   after instance, dF/d(eps) for every design voxel ([n2][n1][n0] order);
+   obj receives F per instance.  On return the instances hold the state
+   after N steps. */
+typedef struct {
+    int32_t lo[3];              /* first voxel of the design box */
+    int32_t n[3];               /* extent in voxels */
+    const double* eps;          /* [n[2]][n[1]][n[0]] eps_inf per voxel, > 0 */
+} sj_design_desc;
+
+typedef struct {
+    int32_t n_cells;            /* cells of the objective patch */
+    const int32_t* cells;       /* [n_cells][3] voxel indices (i, j, k) */
+    int32_t comp_mask;          /* bit c: E component c (1 = Ex, 2 = Ey, 4 = Ez) */
+    int32_t _pad;
+    double frequency;           /* DFT frequency (meep units) */
+} sj_objective_desc;
+
+/* set (or replace) instance inst's design region; NULL removes it */
+int sj_set_design(sj_sim* sim, int32_t inst, const sj_design_desc* design);
+/* objectives[n_instances]; d_obj_d_eps holds every instance's design voxels */
+int sj_adjoint_gradient(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_steps,
+                        int32_t checkpoint_every, double* d_obj_d_eps, size_t cap, double* obj);
+
 /* ---------------------------------------------------------------- rasteriser */
 /* cgs_material_function::in_bound per E-component Yee point, on the device:
    out_masks[3][nz][ny][nx] = bitmask of the scene regions containing the

@@ -63,6 +63,9 @@ def load():
     lib.sjo_rasterize.argtypes = [C.POINTER(_abi.GridDesc), C.POINTER(_abi.SceneDesc),
                                   C.POINTER(C.c_uint8)]
     lib.sjo_csg_in.argtypes = [C.POINTER(_abi.CsgNode), C.c_int, D, C.c_int64, C.POINTER(C.c_uint8)]
+    lib.sjo_set_design.argtypes = [P, C.POINTER(_abi.DesignDesc)]
+    lib.sjo_objective.argtypes = [P, C.POINTER(_abi.ObjectiveDesc), C.c_int64, D]
+    lib.sjo_adjoint.argtypes = [P, C.POINTER(_abi.ObjectiveDesc), C.c_int64, D, D]
     lib.sjo_source_dipole.argtypes = [C.POINTER(_abi.SourceDesc), C.c_double, D, D]
     _lib = lib
     return lib
@@ -93,6 +96,29 @@ class OracleFields:
 
     def step(self, n=1):
         self.lib.sjo_step(self.handle, int(n))
+
+    def set_design(self, design):
+        d, self._design = design.to_c()
+        if self.lib.sjo_set_design(self.handle, C.byref(d)) != 0:
+            raise RuntimeError(self.lib.sjo_last_error().decode())
+
+    def objective(self, objective, n_steps):
+        """F after n_steps from rest."""
+        o, keep = objective.to_c()
+        F = C.c_double()
+        self.lib.sjo_objective(self.handle, C.byref(o), int(n_steps), C.byref(F))
+        return F.value
+
+    def adjoint(self, objective, n_steps):
+        """(F, dF/d eps over the design voxels [k][j][i]) after n_steps from rest."""
+        o, keep = objective.to_c()
+        shape = self._design.shape
+        g = np.zeros(shape, dtype=np.float64)
+        F = C.c_double()
+        if self.lib.sjo_adjoint(self.handle, C.byref(o), int(n_steps), g.ctypes.data_as(C.POINTER(C.c_double)),
+                                C.byref(F)) != 0:
+            raise RuntimeError(self.lib.sjo_last_error().decode())
+        return F.value, g
 
     @property
     def steps_done(self):

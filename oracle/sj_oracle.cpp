@@ -170,6 +170,16 @@ struct sjo_sim {
     int n_mon = 0, n_dft = 0;
     std::vector<std::vector<double>> mon;        // [monitor][samples]
     std::vector<std::complex<double>> dft;       // [dft][freq]
+    // design region: per-voxel inverse eps at the voxel's E points
+    int des_lo[3] = {0, 0, 0}, des_n[3] = {0, 0, 0};
+    std::vector<double> des_inv;                 // [n2][n1][n0]
+    double* rec_acc = nullptr;                   // when set: acc of the E update at design points [d][3]
+
+    long long des_index(int i, int j, int k) const {
+        const int u = i - des_lo[0], v = j - des_lo[1], w = k - des_lo[2];
+        if (des_inv.empty() || u < 0 || v < 0 || w < 0 || u >= des_n[0] || v >= des_n[1] || w >= des_n[2]) return -1;
+        return ((long long)w * des_n[1] + v) * des_n[0] + u;
+    }
 
     long long at(int i, int j, int k) const { return ((long long)k * ny + j) * nx + i; }
 };
@@ -480,10 +490,219 @@ void step_once(sjo_sim* s) {
                         pm = pn;
                         pp = pnew;
                     }
-                    F[ca][o] = eo + s->inv_eps[cl] * acc;
+                    const long long dd = s->des_index(i, j, k);
+                    if (dd >= 0 && s->rec_acc) s->rec_acc[dd * 3 + ca] = acc;
+                    F[ca][o] = eo + (dd >= 0 ? s->des_inv[dd] : s->inv_eps[cl]) * acc;
                 }
             }
     s->t += 1;
+}
+
+// Zero fields, auxiliaries, polarisations, monitors and DFTs; t = 0.
+void reset_state(sjo_sim* s) {
+    for (int c = 0; c < 6; ++c) std::fill(s->F[c].begin(), s->F[c].end(), 0.0);
+    for (int a = 0; a < 3; ++a)
+        for (int q = 0; q < 2; ++q) {
+            std::fill(s->psiE[a][q].begin(), s->psiE[a][q].end(), 0.0);
+            std::fill(s->psiH[a][q].begin(), s->psiH[a][q].end(), 0.0);
+        }
+    for (auto& v : s->P) std::fill(v.begin(), v.end(), 0.0);
+    for (auto& v : s->Pm) std::fill(v.begin(), v.end(), 0.0);
+    for (auto& m : s->mon) m.clear();
+    std::fill(s->dft.begin(), s->dft.end(), std::complex<double>(0.0, 0.0));
+    s->t = 0;
+}
+
+// Objective DFT: D[cell][c] += dt E_c^n(cell) e^{i 2 pi f n dt} for the E
+// components in the mask, sampled before step n.
+void objective_sample(const sjo_sim* s, const sj_objective_desc& ob, long long n,
+                      std::vector<std::complex<double>>& D) {
+    const double th = 2 * M_PI * ob.frequency * (double)n * s->dt;
+    const std::complex<double> w(cos(th) * s->dt, sin(th) * s->dt);
+    for (int q = 0; q < ob.n_cells; ++q) {
+        const int* c3 = ob.cells + 3 * q;
+        const long long o = s->at(c3[0], c3[1], c3[2]);
+        for (int c = 0; c < 3; ++c)
+            if ((ob.comp_mask >> c) & 1) D[3 * q + c] += s->F[c][o] * w;
+    }
+}
+
+// Forward run of n_steps from rest; returns F and, when acc is given, the
+// E-update acc at the design points per step ([n][d][3]).
+double objective_forward(sjo_sim* s, const sj_objective_desc& ob, long long n_steps, double* acc,
+                         std::vector<std::complex<double>>& D) {
+    reset_state(s);
+    D.assign((size_t)3 * ob.n_cells, std::complex<double>(0.0, 0.0));
+    const long long nd = (long long)s->des_inv.size();
+    for (long long n = 0; n < n_steps; ++n) {
+        objective_sample(s, ob, n, D);
+        s->rec_acc = acc ? acc + (size_t)n * nd * 3 : nullptr;
+        step_once(s);
+    }
+    s->rec_acc = nullptr;
+    double F = 0;
+    for (const auto& d : D) F += std::norm(d);
+    return F;
+}
+
+// The discrete adjoint: for n = N-1 .. 0, the transpose of the E update
+// (polarisation ADE, E-side psi, curl of H) and then of the H update
+// (H-side psi, curl of E), plus dF/dE^n from the objective DFT.  Returns
+// dF/d(inverse eps) at the design points ([d][3]).  Gather form: each
+// cell collects the contributions of its neighbours from per-cell arrays.
+void adjoint_sweep(sjo_sim* s, const sj_objective_desc& ob, long long n_steps, const double* acc,
+                   const std::vector<std::complex<double>>& D, std::vector<double>& g) {
+    const int nx = s->nx, ny = s->ny, nz = s->nz;
+    const long long N = s->N;
+    const double S = s->S, dt = s->dt;
+    const long long nd = (long long)s->des_inv.size();
+    std::vector<double> eb[3], hb[3], d1[3], d2[3], psEb[3][2], psHb[3][2];
+    for (int c = 0; c < 3; ++c) {
+        eb[c].assign(N, 0.0), hb[c].assign(N, 0.0), d1[c].assign(N, 0.0), d2[c].assign(N, 0.0);
+        for (int q = 0; q < 2; ++q) psEb[c][q].assign(N, 0.0), psHb[c][q].assign(N, 0.0);
+    }
+    std::vector<std::vector<double>> pb(3 * s->np, std::vector<double>(N, 0.0)), pmb = pb;
+    g.assign((size_t)nd * 3, 0.0);
+    const int nn[3] = {nx, ny, nz};
+    for (long long n = n_steps - 1; n >= 0; --n) {
+        const double* accn = acc + (size_t)n * nd * 3;
+        // ---- transpose of the E update: eb holds dF/dE^{n+1}
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const long long o = s->at(i, j, k);
+                    const int idx[3] = {i, j, k};
+                    const long long dd = s->des_index(i, j, k);
+                    for (int ca = 0; ca < 3; ++ca) {
+                        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+                        const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
+                        const int cl = s->cls[ca][o];
+                        const double inv = dd >= 0 ? s->des_inv[dd] : s->inv_eps[cl];
+                        const double ebo = eb[ca][o];
+                        if (dd >= 0) g[dd * 3 + ca] += ebo * accn[dd * 3 + ca];
+                        const double ab = inv * ebo;
+                        double ein = ebo;
+                        for (int p = 0; p < s->np; ++p) {
+                            const double cs = s->csig[(size_t)cl * s->np + p];
+                            if (cs == 0.0) continue;  // P is never excited there and does not reach E
+                            const double pnb = pb[3 * p + ca][o] - ab;
+                            const double pnbar = pmb[3 * p + ca][o] + ab + s->A[p] * pnb;
+                            pmb[3 * p + ca][o] = s->B[p] * pnb;
+                            pb[3 * p + ca][o] = pnbar;
+                            ein += cs * pnb;
+                        }
+                        eb[ca][o] = ein;
+                        const double cb = S * ab;
+                        double t1 = cb, t2 = -cb;
+                        if (s->oni[a1][idx[a1]]) {
+                            const double t = psEb[a1][s1][o] + cb;
+                            t1 = cb + s->ci[a1][idx[a1]] * t;
+                            psEb[a1][s1][o] = s->bi[a1][idx[a1]] * t;
+                        }
+                        if (s->oni[a2][idx[a2]]) {
+                            const double t = psEb[a2][s2][o] - cb;
+                            t2 = -cb + s->ci[a2][idx[a2]] * t;
+                            psEb[a2][s2][o] = s->bi[a2][idx[a2]] * t;
+                        }
+                        d1[ca][o] = t1;  // adjoint of d1 = H_a2(o) - H_a2(o - e_a1)
+                        d2[ca][o] = t2;  // adjoint of d2 = H_a1(o) - H_a1(o - e_a2)
+                    }
+                }
+        // gather into hb (dF/dH^{n+1/2} = from the future + from this E update)
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const long long o = s->at(i, j, k);
+                    const int idx[3] = {i, j, k};
+                    for (int ca = 0; ca < 3; ++ca) {
+                        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+                        // d1 of E_ca reads H_a2 at o and o - e_a1
+                        double v = d1[ca][o];
+                        if (idx[a1] + 1 < nn[a1]) {
+                            int q[3] = {i, j, k};
+                            q[a1] += 1;
+                            v -= d1[ca][s->at(q[0], q[1], q[2])];
+                        }
+                        hb[a2][o] += v;
+                        // d2 of E_ca reads H_a1 at o and o - e_a2
+                        double w = d2[ca][o];
+                        if (idx[a2] + 1 < nn[a2]) {
+                            int q[3] = {i, j, k};
+                            q[a2] += 1;
+                            w -= d2[ca][s->at(q[0], q[1], q[2])];
+                        }
+                        hb[a1][o] += w;
+                    }
+                }
+        // ---- transpose of the H update: hb holds dF/dH^{n+1/2}; it carries
+        // over unchanged to H^{n-1/2}
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const long long o = s->at(i, j, k);
+                    const int idx[3] = {i, j, k};
+                    for (int ca = 0; ca < 3; ++ca) {
+                        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+                        const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
+                        const double cb = -S * hb[ca][o];
+                        double t1 = cb, t2 = -cb;
+                        if (s->onh[a1][idx[a1]]) {
+                            const double t = psHb[a1][s1][o] + cb;
+                            t1 = cb + s->ch[a1][idx[a1]] * t;
+                            psHb[a1][s1][o] = s->bh[a1][idx[a1]] * t;
+                        }
+                        if (s->onh[a2][idx[a2]]) {
+                            const double t = psHb[a2][s2][o] - cb;
+                            t2 = -cb + s->ch[a2][idx[a2]] * t;
+                            psHb[a2][s2][o] = s->bh[a2][idx[a2]] * t;
+                        }
+                        d1[ca][o] = t1;  // adjoint of d1 = E_a2(o + e_a1) - E_a2(o)
+                        d2[ca][o] = t2;  // adjoint of d2 = E_a1(o + e_a2) - E_a1(o)
+                    }
+                }
+        // gather into eb
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const long long o = s->at(i, j, k);
+                    const int idx[3] = {i, j, k};
+                    for (int ca = 0; ca < 3; ++ca) {
+                        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+                        // H_ca's d1 reads E_a2 at o + e_a1 and o
+                        double v = -d1[ca][o];
+                        if (idx[a1] > 0) {
+                            int q[3] = {i, j, k};
+                            q[a1] -= 1;
+                            v += d1[ca][s->at(q[0], q[1], q[2])];
+                        }
+                        eb[a2][o] += v;
+                        // H_ca's d2 reads E_a1 at o + e_a2 and o
+                        double w = -d2[ca][o];
+                        if (idx[a2] > 0) {
+                            int q[3] = {i, j, k};
+                            q[a2] -= 1;
+                            w += d2[ca][s->at(q[0], q[1], q[2])];
+                        }
+                        eb[a1][o] += w;
+                    }
+                }
+        // ---- dF/dE^n of the objective DFT
+        const double th = 2 * M_PI * ob.frequency * (double)n * dt;
+        const double cth = cos(th), sth = sin(th);
+        for (int q = 0; q < ob.n_cells; ++q) {
+            const int* c3 = ob.cells + 3 * q;
+            const long long o = s->at(c3[0], c3[1], c3[2]);
+            for (int c = 0; c < 3; ++c)
+                if ((ob.comp_mask >> c) & 1) {
+                    const std::complex<double>& d = D[3 * q + c];
+                    eb[c][o] += 2 * dt * (d.real() * cth + d.imag() * sth);
+                }
+        }
+    }
 }
 
 }  // namespace
@@ -579,6 +798,54 @@ int sjo_rasterize(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* out) 
 // CSG inclusion at arbitrary points: out[n] = in_root(point) for one region
 int sjo_csg_in(const sj_csg_node* nodes, int n_nodes, const double* pts, int64_t n_pts, uint8_t* out) {
     for (int64_t q = 0; q < n_pts; ++q) out[q] = (uint8_t)program_in(nodes, n_nodes, pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+    return SJ_OK;
+}
+
+static int fail(const char* msg) {
+    g_err = msg;
+    return SJ_E_INVALID;
+}
+
+int sjo_set_design(sjo_sim* s, const sj_design_desc* d) {
+    if (!d) {
+        s->des_inv.clear();
+        return SJ_OK;
+    }
+    long long nd = 1;
+    for (int a = 0; a < 3; ++a) {
+        const int n = a == 0 ? s->nx : (a == 1 ? s->ny : s->nz);
+        if (d->n[a] < 1 || d->lo[a] < 0 || d->lo[a] + d->n[a] > n) return fail("design box outside the grid");
+        s->des_lo[a] = d->lo[a], s->des_n[a] = d->n[a];
+        nd *= d->n[a];
+    }
+    s->des_inv.resize(nd);
+    for (long long q = 0; q < nd; ++q) {
+        if (!(d->eps[q] > 0)) return fail("design eps must be > 0");
+        s->des_inv[q] = 1.0 / d->eps[q];
+    }
+    return SJ_OK;
+}
+
+// F after n_steps from rest (no gradient)
+int sjo_objective(sjo_sim* s, const sj_objective_desc* ob, int64_t n_steps, double* F) {
+    std::vector<std::complex<double>> D;
+    *F = objective_forward(s, *ob, n_steps, nullptr, D);
+    return SJ_OK;
+}
+
+// F and dF/d(eps) at the design voxels ([d], eps = 1 / inverse eps)
+int sjo_adjoint(sjo_sim* s, const sj_objective_desc* ob, int64_t n_steps, double* grad, double* F) {
+    const long long nd = (long long)s->des_inv.size();
+    if (nd == 0) return fail("no design region");
+    std::vector<double> acc((size_t)n_steps * nd * 3);
+    std::vector<std::complex<double>> D;
+    *F = objective_forward(s, *ob, n_steps, acc.data(), D);
+    std::vector<double> g;
+    adjoint_sweep(s, *ob, n_steps, acc.data(), D, g);
+    for (long long q = 0; q < nd; ++q) {
+        const double inv = s->des_inv[q];
+        grad[q] = -inv * inv * (g[3 * q] + g[3 * q + 1] + g[3 * q + 2]);
+    }
     return SJ_OK;
 }
 

@@ -87,8 +87,17 @@ class InstanceDesc(C.Structure):
                 ("save_span", C.c_int32)]
 
 
+class DesignDesc(C.Structure):
+    _fields_ = [("lo", C.c_int32 * 3), ("n", C.c_int32 * 3), ("eps", C.POINTER(C.c_double))]
+
+
+class ObjectiveDesc(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("cells", C.POINTER(C.c_int32)), ("comp_mask", C.c_int32),
+                ("_pad", C.c_int32), ("frequency", C.c_double)]
+
+
 STRUCTS = {0: GridDesc, 1: Pole, 2: CsgNode, 3: RegionDesc, 4: SceneDesc, 5: MaterialDesc,
-           6: PmlDesc, 7: SourceDesc, 8: ProbeDesc, 9: InstanceDesc}
+           6: PmlDesc, 7: SourceDesc, 8: ProbeDesc, 9: InstanceDesc, 10: DesignDesc, 11: ObjectiveDesc}
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -122,6 +131,8 @@ SIGNATURES = {
     "sj_bytes_per_step": (C.c_double, [_P, C.c_int32]),
     "sj_launches_per_step": (C.c_int32, [_P]),
     "sj_get_schedule": (C.c_int32, [_P]),
+    "sj_set_design": (C.c_int, [_P, C.c_int32, C.POINTER(DesignDesc)]),
+    "sj_adjoint_gradient": (C.c_int, [_P, C.POINTER(ObjectiveDesc), C.c_int64, C.c_int32, _D, C.c_size_t, _D]),
     "sj_read_monitors": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_dft": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

@@ -1102,6 +1102,8 @@ int64_t sj_abi_struct_size(int32_t which) {
         case 7: return sizeof(sj_source_desc);
         case 8: return sizeof(sj_probe_desc);
         case 9: return sizeof(sj_instance_desc);
+        case 10: return sizeof(sj_design_desc);
+        case 11: return sizeof(sj_objective_desc);
         default: return -1;
     }
 }

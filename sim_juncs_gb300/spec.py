@@ -216,3 +216,39 @@ def scene_to_c(scene, holder=None):
     inst = Instance(Grid(1, 1, 1, 1.0), scene)
     d, h = inst.to_c(holder)
     return d.material.scene, h
+
+
+@dataclass
+class Design:
+    """A design region: per-voxel eps_inf on the box lo .. lo + eps.shape[::-1]
+    (eps indexed [k][j][i]), applied at each voxel's Ex, Ey and Ez points."""
+    lo: Tuple[int, int, int]
+    eps: np.ndarray
+
+    def to_c(self):
+        eps = np.ascontiguousarray(self.eps, dtype=np.float64)
+        assert eps.ndim == 3
+        d = _abi.DesignDesc()
+        for a in range(3):
+            d.lo[a] = int(self.lo[a])
+            d.n[a] = int(eps.shape[2 - a])
+        d.eps = eps.ctypes.data_as(C.POINTER(C.c_double))
+        return d, eps
+
+
+@dataclass
+class Objective:
+    """F = sum over `cells` and E components `comps` of |DFT_f(E_c)|^2, the
+    DFT summed over the run (dt E^n e^{+i 2 pi f n dt}, sampled before step n)."""
+    cells: np.ndarray                  # [n][3] voxel indices (i, j, k)
+    frequency: float
+    comps: Tuple[int, ...] = (0, 1, 2)
+
+    def to_c(self):
+        cells = np.ascontiguousarray(self.cells, dtype=np.int32).reshape(-1, 3)
+        o = _abi.ObjectiveDesc()
+        o.n_cells = len(cells)
+        o.cells = cells.ctypes.data_as(C.POINTER(C.c_int32))
+        o.comp_mask = sum(1 << c for c in self.comps)
+        o.frequency = float(self.frequency)
+        return o, cells
