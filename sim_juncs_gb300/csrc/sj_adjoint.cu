@@ -1,0 +1,223 @@
+// Discrete adjoint of the split schedule's step, and the objective DFT.
+//
+// The step is linear in the fields with coefficients that do not depend on
+// them (S, eps_inf^{-1}, the CPML b and c, the ADE's A, B and C sigma), so
+// its adjoint is the reverse sequence of the transposed sub-updates, with the
+// same coefficients: for step n, first the transpose of the E update
+// (eps_inf^{-1}, the polarisation ADE, the E-side psi, the backward
+// differences of H), then the transpose of the H update (the H-side psi and
+// the forward differences of E).  A difference's adjoint is scattered to the
+// two cells it reads; each kernel pair writes the per-cell adjoints of both
+// differences (t1, t2) and then gathers them, one thread per cell, so no two
+// threads write one value.  The gradient with respect to a design voxel's
+// inverse eps is sum_n dF/dE^{n+1} * acc^n, acc^n being the E update's
+// bracket at step n, recorded while the segment is re-run forward.
+// One launch per instance; the descriptor travels as a kernel parameter.
+#include "sj_physics.cuh"
+
+namespace sj {
+
+namespace {
+
+constexpr int AX = 32, AY = 8;
+
+template <typename real>
+__device__ __forceinline__ real prof_at(const InstDev<real>& I, int a, int q, int which) {
+    // which: 0 = b (integer points), 1 = c (integer), 2 = b (half), 3 = c (half)
+    return I.prof[a][which * dim_of(I, a) + q];
+}
+
+template <typename real>
+__device__ __forceinline__ long long stride_of(const InstDev<real>& I, int a) {
+    return a == 0 ? 1LL : (a == 1 ? (long long)I.px : I.plane);
+}
+
+template <typename real>
+__device__ __forceinline__ long long design_index(const InstDev<real>& I, int i, int j, int k) {
+    if (!I.dinv) return -1;
+    const int u = i - I.des_lo[0], v = j - I.des_lo[1], w = k - I.des_lo[2];
+    if ((unsigned)u >= (unsigned)I.des_n[0] || (unsigned)v >= (unsigned)I.des_n[1] ||
+        (unsigned)w >= (unsigned)I.des_n[2])
+        return -1;
+    return ((long long)w * I.des_n[1] + v) * I.des_n[0] + u;
+}
+
+// Transpose of the E update at one voxel (three components).  eb holds
+// dF/dE^{n+1} on entry and the E update's share of dF/dE^n on exit.
+template <typename real>
+__global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDev<real> A, long long n) {
+    const InstDev<real>& I = A.I;
+    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
+    if (i >= I.nx || j >= I.ny) return;
+    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+    const int idx[3] = {i, j, k};
+    const int cb = I.combo[o];
+    const real* cf = I.coef + cb * I.ncoef;
+    const bool disp = (I.cflag[cb] & 1) != 0;
+    const long long di =
+        disp ? ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]) : 0;
+    const long long d = design_index(I, i, j, k);
+    const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
+    for (int ca = 0; ca < 3; ++ca) {
+        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+        const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
+        const real inv = d >= 0 ? I.dinv[d] : cf[ca];
+        const real ebo = A.eb[ca][o];
+        if (d >= 0) A.g[d * 3 + ca] += (double)ebo * (double)A.rec[((n - A.rec_t0) * nd + d) * 3 + ca];
+        const real ab = inv * ebo;  // adjoint of the bracket acc
+        real ein = ebo;
+        if (disp)
+            for (int p = 0; p < I.n_poles; ++p) {
+                const real cs = cf[3 + 3 * p + ca];
+                if (cs == real(0)) continue;  // P is never excited there and does not reach E
+                real* p0 = A.pb + ((long long)(p * 2 + 0) * 3 + ca) * I.dvol + di;
+                real* p1 = A.pb + ((long long)(p * 2 + 1) * 3 + ca) * I.dvol + di;
+                const real pnb = *p0 - ab;                    // dF/dP^{n+1}
+                const real pn = *p1 + ab + I.A[p] * pnb;      // dF/dP^n
+                *p1 = I.B[p] * pnb;                           // dF/dP^{n-1}
+                *p0 = pn;
+                ein += cs * pnb;
+            }
+        A.eb[ca][o] = ein;
+        const real cv = I.S * ab;  // adjoint of the curl
+        real t1 = cv, t2 = -cv;
+        if (in_slab(I, a1, idx[a1])) {
+            real* ps = A.psEb[a1] + (long long)s1 * I.vol + o;
+            const real t = *ps + cv;
+            t1 = cv + prof_at(I, a1, idx[a1], 1) * t;
+            *ps = prof_at(I, a1, idx[a1], 0) * t;
+        }
+        if (in_slab(I, a2, idx[a2])) {
+            real* ps = A.psEb[a2] + (long long)s2 * I.vol + o;
+            const real t = *ps - cv;
+            t2 = -cv + prof_at(I, a2, idx[a2], 1) * t;
+            *ps = prof_at(I, a2, idx[a2], 0) * t;
+        }
+        A.t1[ca][o] = t1;  // adjoint of H_a2(o) - H_a2(o - e_a1)
+        A.t2[ca][o] = t2;  // adjoint of H_a1(o) - H_a1(o - e_a2)
+    }
+}
+
+// dF/dH^{n+1/2} += what the E update's differences read from H at this cell.
+template <typename real>
+__global__ void __launch_bounds__(AX * AY) k_adj_e_gather(const __grid_constant__ AdjDev<real> A) {
+    const InstDev<real>& I = A.I;
+    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
+    if (i >= I.nx || j >= I.ny) return;
+    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+    const int idx[3] = {i, j, k};
+    for (int ca = 0; ca < 3; ++ca) {
+        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+        real v = A.t1[ca][o];
+        if (idx[a1] + 1 < dim_of(I, a1)) v -= A.t1[ca][o + stride_of(I, a1)];
+        A.hb[a2][o] += v;
+        real w = A.t2[ca][o];
+        if (idx[a2] + 1 < dim_of(I, a2)) w -= A.t2[ca][o + stride_of(I, a2)];
+        A.hb[a1][o] += w;
+    }
+}
+
+// Transpose of the H update: hb (dF/dH^{n+1/2}) carries over unchanged to
+// H^{n-1/2}; its share through the curl of E goes to t1, t2.
+template <typename real>
+__global__ void __launch_bounds__(AX * AY) k_adj_h(const __grid_constant__ AdjDev<real> A) {
+    const InstDev<real>& I = A.I;
+    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
+    if (i >= I.nx || j >= I.ny) return;
+    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+    const int idx[3] = {i, j, k};
+    for (int ca = 0; ca < 3; ++ca) {
+        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+        const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
+        const real cv = -I.S * A.hb[ca][o];
+        real t1 = cv, t2 = -cv;
+        if (in_slab(I, a1, idx[a1])) {
+            real* ps = A.psHb[a1] + (long long)s1 * I.vol + o;
+            const real t = *ps + cv;
+            t1 = cv + prof_at(I, a1, idx[a1], 3) * t;
+            *ps = prof_at(I, a1, idx[a1], 2) * t;
+        }
+        if (in_slab(I, a2, idx[a2])) {
+            real* ps = A.psHb[a2] + (long long)s2 * I.vol + o;
+            const real t = *ps - cv;
+            t2 = -cv + prof_at(I, a2, idx[a2], 3) * t;
+            *ps = prof_at(I, a2, idx[a2], 2) * t;
+        }
+        A.t1[ca][o] = t1;  // adjoint of E_a2(o + e_a1) - E_a2(o)
+        A.t2[ca][o] = t2;  // adjoint of E_a1(o + e_a2) - E_a1(o)
+    }
+}
+
+// dF/dE^n += what the H update's differences read from E at this cell.
+template <typename real>
+__global__ void __launch_bounds__(AX * AY) k_adj_h_gather(const __grid_constant__ AdjDev<real> A) {
+    const InstDev<real>& I = A.I;
+    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
+    if (i >= I.nx || j >= I.ny) return;
+    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+    const int idx[3] = {i, j, k};
+    for (int ca = 0; ca < 3; ++ca) {
+        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+        real v = -A.t1[ca][o];
+        if (idx[a1] > 0) v += A.t1[ca][o - stride_of(I, a1)];
+        A.eb[a2][o] += v;
+        real w = -A.t2[ca][o];
+        if (idx[a2] > 0) w += A.t2[ca][o - stride_of(I, a2)];
+        A.eb[a1][o] += w;
+    }
+}
+
+// One thread per (objective cell, E component in the mask).
+template <typename real>
+__global__ void k_objective(const __grid_constant__ InstDev<real> I, int cur, const int* __restrict__ cells,
+                            int n_cells, int mask, double freq, double2* D, long long n, int sample,
+                            real* ebx, real* eby, real* ebz) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = t / 3, c = t % 3;
+    if (q >= n_cells || !((mask >> c) & 1)) return;
+    const long long o = (long long)cells[3 * q + 2] * I.plane + (long long)cells[3 * q + 1] * I.px + cells[3 * q];
+    double sn, cs;
+    sincospi(2.0 * freq * ((double)n * I.dt), &sn, &cs);
+    if (sample) {
+        const double e = (double)I.F[cur][c][o] * I.dt;
+        double2 v = D[t];
+        v.x += e * cs;
+        v.y += e * sn;
+        D[t] = v;
+    } else {
+        real* eb = c == 0 ? ebx : (c == 1 ? eby : ebz);
+        const double2 v = D[t];
+        eb[o] += (real)(2.0 * I.dt * (v.x * cs + v.y * sn));
+    }
+}
+
+}  // namespace
+
+template <typename real>
+cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, cudaStream_t s) {
+    const dim3 block(AX, AY), grid((a.I.nx + AX - 1) / AX, (a.I.ny + AY - 1) / AY, a.I.nz);
+    k_adj_e<real><<<grid, block, 0, s>>>(a, n);
+    k_adj_e_gather<real><<<grid, block, 0, s>>>(a);
+    k_adj_h<real><<<grid, block, 0, s>>>(a);
+    k_adj_h_gather<real><<<grid, block, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells, int n_cells, int comp_mask,
+                             double freq, double2* d_D, long long n, bool sample, real* const* eb, cudaStream_t s) {
+    const int threads = 3 * n_cells;
+    if (threads == 0) return cudaSuccess;
+    k_objective<real><<<(threads + 127) / 128, 128, 0, s>>>(I, cur, d_cells, n_cells, comp_mask, freq, d_D, n,
+                                                            sample ? 1 : 0, eb ? eb[0] : nullptr,
+                                                            eb ? eb[1] : nullptr, eb ? eb[2] : nullptr);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_adjoint_step<float>(const AdjDev<float>&, long long, cudaStream_t);
+template cudaError_t launch_adjoint_step<double>(const AdjDev<double>&, long long, cudaStream_t);
+template cudaError_t launch_objective<float>(const InstDev<float>&, int, const int*, int, int, double, double2*,
+                                             long long, bool, float* const*, cudaStream_t);
+template cudaError_t launch_objective<double>(const InstDev<double>&, int, const int*, int, int, double, double2*,
+                                              long long, bool, double* const*, cudaStream_t);
+}  // namespace sj

@@ -110,6 +110,8 @@ struct HostInst {
     double* d_mon = nullptr;
     long long mon_cap = 0;
     std::vector<uint32_t> keys;      // combo -> (cx | cy<<8 | cz<<16)
+    std::vector<double> des_eps;     // design region eps per voxel (empty: none)
+    real* d_dinv = nullptr;          // its inverse on the device
     long long voxels = 0;
     double bytes_per_step = 0;
     double last_source_time = 0;
@@ -1073,6 +1075,237 @@ void write_field_t(sj_sim* sim, int inst, int comp, const double* in) {
        "field write");
 }
 
+// ------------------------------------------------------------------ adjoint
+template <typename real>
+bool any_design(sj_sim* sim) {
+    for (const auto& H : hostv<real>(sim))
+        if (!H.des_eps.empty()) return true;
+    return false;
+}
+
+template <typename real>
+void set_design_t(sj_sim* sim, int q, const sj_design_desc* d) {
+    HostInst<real>& H = hostv<real>(sim)[q];
+    InstDev<real>& I = devv<real>(sim)[q];
+    long long nd = 1;
+    if (d) {
+        const int n3[3] = {H.nx, H.ny, H.nz};
+        for (int a = 0; a < 3; ++a) {
+            if (d->n[a] < 1 || d->lo[a] < 0 || (long long)d->lo[a] + d->n[a] > n3[a])
+                fail(SJ_E_INVALID, "design box outside the grid");
+            nd *= d->n[a];
+        }
+        if (!d->eps) fail(SJ_E_INVALID, "design eps is NULL");
+        for (long long k = 0; k < nd; ++k)
+            if (!(d->eps[k] > 0) || !std::isfinite(d->eps[k])) fail(SJ_E_INVALID, "design eps must be finite and > 0");
+    }
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    sim->dfree(H.d_dinv);
+    H.d_dinv = nullptr;
+    H.des_eps.clear();
+    I.dinv = nullptr;
+    for (int a = 0; a < 3; ++a) I.des_lo[a] = I.des_n[a] = 0;
+    if (d) {
+        H.des_eps.assign(d->eps, d->eps + nd);
+        std::vector<real> inv(nd);
+        for (long long k = 0; k < nd; ++k) inv[k] = (real)(1.0 / d->eps[k]);
+        H.d_dinv = sim->upload(inv);
+        I.dinv = H.d_dinv;
+        for (int a = 0; a < 3; ++a) I.des_lo[a] = d->lo[a], I.des_n[a] = d->n[a];
+        // the per-voxel eps is applied by the split schedule's E update
+        sim->schedule = SJ_SCHED_SPLIT;
+    }
+    sim->drop_graphs();
+    upload_table<real>(sim);
+}
+
+template <typename real>
+void set_dev_step(sj_sim* sim, long long step) {
+    DevState st{};
+    st.step = step;
+    st.done = 0;
+    st.cur = sim->cur;
+    st.status = 0;
+    ck(cudaMemcpyAsync(sim->d_state, &st, sizeof(st), cudaMemcpyHostToDevice, sim->stream), "state");
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+}
+
+template <typename real>
+void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long long K, double* grad, size_t cap,
+               double* objv) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    const int ni = sim->n_inst;
+    if (N < 1) fail(SJ_E_INVALID, "n_steps must be >= 1");
+    if (!objs || !objv) fail(SJ_E_INVALID, "objectives and obj must not be NULL");
+    if (K < 1 || K > N) K = N;
+    long long total_d = 0;
+    for (int q = 0; q < ni; ++q) {
+        const sj_objective_desc& ob = objs[q];
+        if (ob.n_cells < 0 || (ob.n_cells > 0 && !ob.cells)) fail(SJ_E_INVALID, "bad objective cells");
+        if (ob.comp_mask < 1 || ob.comp_mask > 7) fail(SJ_E_INVALID, "objective comp_mask must be in 1..7");
+        for (int c = 0; c < ob.n_cells; ++c) {
+            const int* x = ob.cells + 3 * c;
+            if (x[0] < 0 || x[1] < 0 || x[2] < 0 || x[0] >= hv[q].nx || x[1] >= hv[q].ny || x[2] >= hv[q].nz)
+                fail(SJ_E_INVALID, "objective cell outside the grid");
+        }
+        total_d += (long long)hv[q].des_eps.size();
+    }
+    if (total_d > 0 && (!grad || (size_t)total_d > cap)) fail(SJ_E_RANGE, "d_obj_d_eps too small for the design voxels");
+    sim->schedule = SJ_SCHED_SPLIT;
+    sim->drop_graphs();
+    ensure_capacity<real>(sim, N);
+    cudaStream_t st = sim->stream;
+    const int cur = sim->cur;
+    std::vector<void*> temps;  // freed at the end
+    auto tmp = [&](size_t bytes) {
+        void* p = sim->dalloc(bytes);
+        temps.push_back(p);
+        return p;
+    };
+    // ---- the state one step needs: fields, psi, polarisations
+    struct Arr {
+        void* p;
+        size_t bytes;
+    };
+    std::vector<Arr> state;
+    for (int q = 0; q < ni; ++q) {
+        const InstDev<real>& I = dv[q];
+        const size_t vb = (size_t)I.vol * sizeof(real);
+        for (int c = 0; c < 6; ++c) state.push_back({I.F[cur][c], vb});
+        for (int a = 0; a < 3; ++a)
+            if (I.psiE[a]) state.push_back({I.psiE[a], 2 * vb}), state.push_back({I.psiH[cur][a], 2 * vb});
+        if (I.P) state.push_back({I.P, (size_t)I.n_poles * 6 * I.dvol * sizeof(real)});
+    }
+    size_t sbytes = 0;
+    for (const Arr& a : state) sbytes += a.bytes;
+    const long long nseg = (N + K - 1) / K;
+    char* arena = (char*)tmp((size_t)(nseg + 1) * sbytes);
+    auto save = [&](long long slot) {
+        size_t off = (size_t)slot * sbytes;
+        for (const Arr& a : state) {
+            ck(cudaMemcpyAsync(arena + off, a.p, a.bytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+            off += a.bytes;
+        }
+    };
+    auto restore = [&](long long slot) {
+        size_t off = (size_t)slot * sbytes;
+        for (const Arr& a : state) {
+            ck(cudaMemcpyAsync(a.p, arena + off, a.bytes, cudaMemcpyDeviceToDevice, st), "restore");
+            off += a.bytes;
+        }
+    };
+    // ---- objective cells and DFT sums
+    std::vector<int*> d_cells(ni, nullptr);
+    std::vector<double2*> d_D(ni, nullptr);
+    for (int q = 0; q < ni; ++q) {
+        const int nc = objs[q].n_cells;
+        if (nc == 0) continue;
+        d_cells[q] = (int*)tmp((size_t)nc * 3 * sizeof(int));
+        ck(cudaMemcpyAsync(d_cells[q], objs[q].cells, (size_t)nc * 3 * sizeof(int), cudaMemcpyHostToDevice, st),
+           "cells");
+        d_D[q] = (double2*)tmp((size_t)nc * 3 * sizeof(double2));
+    }
+    // ---- forward from rest, keeping the state every K steps and at the end
+    for (const Arr& a : state) ck(cudaMemsetAsync(a.p, 0, a.bytes, st), "reset");
+    for (int q = 0; q < ni; ++q)
+        if (dv[q].dft) ck(cudaMemsetAsync(dv[q].dft, 0, (size_t)hv[q].n_dft * hv[q].n_freq * sizeof(double2), st), "reset");
+    sim->t = 0;
+    set_dev_step<real>(sim, 0);
+    for (long long n = 0; n < N; ++n) {
+        if (n % K == 0) save(n / K);
+        for (int q = 0; q < ni; ++q)
+            ck(launch_objective<real>(dv[q], cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask, objs[q].frequency,
+                                      d_D[q], n, true, nullptr, st),
+               "objective");
+        ck(launch_one<real>(sim), "step launch");
+    }
+    save(nseg);
+    std::vector<std::vector<double2>> dft_keep(ni);
+    ck(cudaStreamSynchronize(st), "sync");
+    for (int q = 0; q < ni; ++q) {
+        if (dv[q].dft) {
+            dft_keep[q].resize((size_t)hv[q].n_dft * hv[q].n_freq);
+            ck(cudaMemcpy(dft_keep[q].data(), dv[q].dft, dft_keep[q].size() * sizeof(double2), cudaMemcpyDeviceToHost),
+               "dft");
+        }
+        double F = 0;
+        if (objs[q].n_cells) {
+            std::vector<double2> D((size_t)objs[q].n_cells * 3);
+            ck(cudaMemcpy(D.data(), d_D[q], D.size() * sizeof(double2), cudaMemcpyDeviceToHost), "objective");
+            for (const double2& v : D) F += v.x * v.x + v.y * v.y;
+        }
+        objv[q] = F;
+    }
+    // ---- adjoint buffers
+    std::vector<AdjDev<real>> A(ni);
+    for (int q = 0; q < ni; ++q) {
+        const InstDev<real>& I = dv[q];
+        AdjDev<real>& a = A[q];
+        memset(&a, 0, sizeof(a));
+        a.I = I;
+        const size_t vb = (size_t)I.vol * sizeof(real);
+        for (int c = 0; c < 3; ++c) {
+            a.eb[c] = (real*)tmp(vb);
+            a.hb[c] = (real*)tmp(vb);
+            a.t1[c] = (real*)tmp(vb);
+            a.t2[c] = (real*)tmp(vb);
+        }
+        for (int ax = 0; ax < 3; ++ax)
+            if (I.psiE[ax]) a.psEb[ax] = (real*)tmp(2 * vb), a.psHb[ax] = (real*)tmp(2 * vb);
+        if (I.P) a.pb = (real*)tmp((size_t)I.n_poles * 6 * I.dvol * sizeof(real));
+        const long long nd = (long long)hv[q].des_eps.size();
+        if (nd) {
+            a.rec = (const real*)tmp((size_t)K * nd * 3 * sizeof(real));
+            a.g = (double*)tmp((size_t)nd * 3 * sizeof(double));
+        }
+    }
+    // ---- backwards, one segment at a time: re-run it forward recording acc
+    // at the design points, then its transposed steps in reverse
+    for (long long seg = nseg - 1; seg >= 0; --seg) {
+        const long long t0 = seg * K, t1 = std::min(N, t0 + K);
+        restore(seg);
+        sim->t = t0;
+        set_dev_step<real>(sim, t0);
+        for (int q = 0; q < ni; ++q)
+            if (A[q].rec) dv[q].rec_acc = const_cast<real*>(A[q].rec), dv[q].rec_t0 = t0, dv[q].rec_len = t1 - t0;
+        upload_table<real>(sim);
+        for (long long n = t0; n < t1; ++n) ck(launch_one<real>(sim), "step launch");
+        for (int q = 0; q < ni; ++q) dv[q].rec_acc = nullptr, dv[q].rec_len = 0;
+        upload_table<real>(sim);
+        for (long long n = t1 - 1; n >= t0; --n)
+            for (int q = 0; q < ni; ++q) {
+                A[q].rec_t0 = t0;
+                ck(launch_adjoint_step<real>(A[q], n, st), "adjoint step");
+                ck(launch_objective<real>(dv[q], cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask,
+                                          objs[q].frequency, d_D[q], n, false, A[q].eb, st),
+                   "adjoint source");
+            }
+    }
+    // ---- back to the state after N steps
+    restore(nseg);
+    sim->t = N;
+    set_dev_step<real>(sim, N);
+    for (int q = 0; q < ni; ++q)
+        if (dv[q].dft)
+            ck(cudaMemcpy(dv[q].dft, dft_keep[q].data(), dft_keep[q].size() * sizeof(double2), cudaMemcpyHostToDevice),
+               "dft");
+    // ---- dF/d(eps) = -eps^{-2} sum_c dF/d(inverse eps at the voxel's E_c point)
+    long long off = 0;
+    for (int q = 0; q < ni; ++q) {
+        const long long nd = (long long)hv[q].des_eps.size();
+        if (!nd) continue;
+        std::vector<double> g((size_t)nd * 3);
+        ck(cudaMemcpy(g.data(), A[q].g, g.size() * sizeof(double), cudaMemcpyDeviceToHost), "gradient");
+        for (long long d = 0; d < nd; ++d) {
+            const double e = hv[q].des_eps[d];
+            grad[off + d] = -(g[3 * d] + g[3 * d + 1] + g[3 * d + 2]) / (e * e);
+        }
+        off += nd;
+    }
+    for (void* p : temps) sim->dfree(p);
+}
+
 template <typename real>
 void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
     auto& hv = hostv<real>(sim);
@@ -1172,8 +1405,32 @@ int sj_set_schedule(sj_sim* sim, int32_t schedule) {
     if (!sim) return SJ_E_INVALID;
     if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT && schedule != SJ_SCHED_TMA)
         return finish(sim, SJ_E_INVALID, "unknown schedule");
+    const bool des = sim->precision == SJ_F64 ? any_design<double>(sim) : any_design<float>(sim);
+    if (des && schedule != SJ_SCHED_SPLIT)
+        return finish(sim, SJ_E_INVALID, "instances with a design region step with the split schedule");
     sim->schedule = schedule;
     return SJ_OK;
+}
+
+int sj_set_design(sj_sim* sim, int32_t inst, const sj_design_desc* design) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        set_design_t<double>(sim, inst, design);
+    else
+        set_design_t<float>(sim, inst, design);
+    SJ_CATCH(sim)
+}
+
+int sj_adjoint_gradient(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_steps, int32_t checkpoint_every,
+                        double* d_obj_d_eps, size_t cap, double* obj) {
+    if (!sim) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        adjoint_t<double>(sim, objectives, n_steps, checkpoint_every, d_obj_d_eps, cap, obj);
+    else
+        adjoint_t<float>(sim, objectives, n_steps, checkpoint_every, d_obj_d_eps, cap, obj);
+    SJ_CATCH(sim)
 }
 
 int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {

@@ -71,6 +71,13 @@ struct InstDev {
     long long mon_cap;
     double2* dft;               // [n_dft][n_freq]
 
+    // design region (adjoint): per-voxel inverse eps at the voxel's E points,
+    // and, while a segment is re-run, the E-update acc recorded there
+    const real* dinv;           // [des_n2][des_n1][des_n0], null without a design region
+    int des_lo[3], des_n[3];
+    real* rec_acc;              // [step - rec_t0][design voxel][3], null when not recording
+    long long rec_t0, rec_len;
+
     // fused schedule: TMA descriptors and tiling
     const void* tmap;           // 31 CUtensorMap: E[b][c], H[b][c], combo, psiE[a][p], psiH[b][a][p]
     int f_ntx, f_nty, f_nzs, f_zs;  // tiles in x, y; z segments and their length
@@ -168,6 +175,29 @@ int fused_smem_bytes(int ty, int ring);  // dynamic shared memory of a tiling, -
 constexpr int FUSED_MAX_SMEM = 227 * 1024;
 template <typename real>
 cudaError_t launch_max_abs_e(const InstDev<real>& h_inst, int buf, double* d_out, cudaStream_t s);
+
+// Adjoint (sj_adjoint.cu): the transposed step of one instance.
+template <typename real>
+struct AdjDev {
+    InstDev<real> I;            // coefficients, geometry, design region
+    real* eb[3];                // dF/dE
+    real* hb[3];                // dF/dH
+    real* t1[3];                // per component: adjoint of its first difference
+    real* t2[3];                // ... and of its second
+    real* psEb[3];              // [axis] -> [2 slots][vol] (null where the axis has no slab)
+    real* psHb[3];
+    real* pb;                   // polarisation layout: level 0 = dF/dP^n, level 1 = dF/dP^{n-1}
+    const real* rec;            // E-update acc at the design points, [step - rec_t0][d][3]
+    long long rec_t0;
+    double* g;                  // dF/d(inverse eps) at the design points [d][3]
+};
+template <typename real>
+cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, cudaStream_t s);
+// Objective DFT of one instance: D[q][c] += dt E_c^n(cell q) e^{i 2 pi f n dt}
+// (sample = true, from buffer cur) or dF/dE^n source into eb (sample = false).
+template <typename real>
+cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells, int n_cells, int comp_mask,
+                             double freq, double2* d_D, long long n, bool sample, real* const* eb, cudaStream_t s);
 
 // Launch helpers implemented in sj_raster.cu.
 cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_start,

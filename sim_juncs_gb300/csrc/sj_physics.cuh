@@ -101,7 +101,20 @@ __device__ __forceinline__ real e_finish(const InstDev<real>& I, int i, int j, i
             }
         }
     }
-    return e_old + cf[CA] * acc;
+    real inv = cf[CA];
+    if (I.dinv) {  // design region: per-voxel inverse eps; acc recorded while a segment is re-run
+        const int u = i - I.des_lo[0], v = j - I.des_lo[1], w = k - I.des_lo[2];
+        if ((unsigned)u < (unsigned)I.des_n[0] && (unsigned)v < (unsigned)I.des_n[1] &&
+            (unsigned)w < (unsigned)I.des_n[2]) {
+            const long long d = ((long long)w * I.des_n[1] + v) * I.des_n[0] + u;
+            inv = I.dinv[d];
+            if (store && I.rec_acc && n >= I.rec_t0 && n < I.rec_t0 + I.rec_len) {
+                const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
+                I.rec_acc[((n - I.rec_t0) * nd + d) * 3 + CA] = acc;
+            }
+        }
+    }
+    return e_old + inv * acc;
 }
 
 // e_finish with the combo's coefficient row (cf) and dispersion flag supplied

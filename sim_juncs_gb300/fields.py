@@ -38,6 +38,7 @@ class Fields:
         _abi.check(self.lib, self.lib.sj_batch_create(n, descs, self.precision, C.byref(handle)))
         self.handle = handle
         self._holders = None  # the library copied everything it needs
+        self._designs = {}    # instance -> design eps shape
         if schedule is not None:  # default: fused for f32, split for f64
             self.set_schedule(schedule)
         if stream is not None:
@@ -134,6 +135,44 @@ class Fields:
         if inst is None:
             return sum(self.lib.sj_bytes_per_step(self.handle, q) for q in range(self.n_instances))
         return self.lib.sj_bytes_per_step(self.handle, inst)
+
+    # ------------------------------------------------------------ adjoint
+    def set_design(self, design, inst=0):
+        """Per-voxel eps on a box (spec.Design), or None to remove it.  An
+        instance with a design region steps with the split schedule."""
+        if design is None:
+            self._ck(self.lib.sj_set_design(self.handle, inst, None))
+            self._designs.pop(inst, None)
+            return
+        d, keep = design.to_c()
+        self._ck(self.lib.sj_set_design(self.handle, inst, C.byref(d)))
+        self._designs[inst] = keep.shape
+
+    def adjoint_gradient(self, objectives, n_steps, checkpoint_every=200):
+        """Run n_steps from rest and the discrete adjoint back.  objectives:
+        one spec.Objective per instance (or one for a single instance).
+        Returns (F per instance, dF/d eps per instance shaped like its design
+        eps, None where it has no design region)."""
+        if not isinstance(objectives, (list, tuple)):
+            objectives = [objectives]
+        assert len(objectives) == self.n_instances
+        arr = (_abi.ObjectiveDesc * self.n_instances)()
+        keep = []
+        for q, ob in enumerate(objectives):
+            o, k = ob.to_c()
+            arr[q] = o
+            keep.append(k)
+        sizes = [int(np.prod(self._designs[q])) if q in self._designs else 0 for q in range(self.n_instances)]
+        g = np.zeros(max(1, sum(sizes)), dtype=np.float64)
+        F = np.zeros(self.n_instances, dtype=np.float64)
+        self._ck(self.lib.sj_adjoint_gradient(self.handle, arr, int(n_steps), int(checkpoint_every),
+                                              g.ctypes.data_as(C.POINTER(C.c_double)), g.size,
+                                              F.ctypes.data_as(C.POINTER(C.c_double))))
+        out, off = [], 0
+        for q, n in enumerate(sizes):
+            out.append(g[off:off + n].reshape(self._designs[q]).copy() if n else None)
+            off += n
+        return F, out
 
     def schedule_name(self):
         """The schedule in use: "fused", "split" or "tma"."""

@@ -1,0 +1,111 @@
+"""The CUDA adjoint (sj_adjoint_gradient) against the oracle's FP64 adjoint,
+which test_adjoint_cpu.py checks against finite differences."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleFields
+from sim_juncs_gb300 import _abi
+from sim_juncs_gb300.fields import Fields
+from sim_juncs_gb300.spec import Design
+
+from test_adjoint_cpu import N_STEPS, setup
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(scope="module")
+def reference():
+    inst, des, obj = setup()
+    o = OracleFields(inst)
+    o.set_design(des)
+    F, g = o.adjoint(obj, N_STEPS)
+    return F, g
+
+
+def test_f64_adjoint_matches_oracle(lib, oracle_lib, reference):
+    inst, des, obj = setup()
+    f = Fields(inst, "f64")
+    f.set_design(des)
+    F, g = f.adjoint_gradient(obj, N_STEPS, checkpoint_every=50)
+    assert F[0] == pytest.approx(reference[0], rel=1e-10)
+    assert rel(g[0], reference[1]) <= 1e-8
+
+
+def test_f32_adjoint_within_1e3_of_f64(lib, oracle_lib, reference):
+    inst, des, obj = setup()
+    f = Fields(inst, "f32")
+    f.set_design(des)
+    F, g = f.adjoint_gradient(obj, N_STEPS, checkpoint_every=50)
+    assert F[0] == pytest.approx(reference[0], rel=1e-4)
+    assert rel(g[0], reference[1]) <= 1e-3, rel(g[0], reference[1])
+
+
+def test_checkpoint_interval_changes_nothing(lib):
+    inst, des, obj = setup()
+    out = []
+    for K in (16, 37, N_STEPS):
+        f = Fields(inst, "f32")
+        f.set_design(des)
+        out.append(f.adjoint_gradient(obj, N_STEPS, checkpoint_every=K))
+        f.close()
+    for F, g in out[1:]:
+        assert F[0] == out[0][0][0]
+        np.testing.assert_array_equal(g[0], out[0][1][0])
+
+
+def test_state_after_adjoint_equals_plain_stepping(lib):
+    inst, des, obj = setup()
+    a = Fields(inst, "f64")
+    a.set_design(des)
+    a.adjoint_gradient(obj, N_STEPS, checkpoint_every=40)
+    b = Fields(inst, "f64")
+    b.set_design(des)
+    b.step(N_STEPS)
+    assert a.steps_done == b.steps_done == N_STEPS
+    for c in range(6):
+        np.testing.assert_array_equal(a.get_array(c), b.get_array(c))
+    np.testing.assert_array_equal(a.monitors(), b.monitors())
+
+
+def test_batched_designs_equal_separate_runs(lib):
+    inst, des, obj = setup()
+    des2 = Design(des.lo, des.eps[::-1, ::-1, :].copy() * 0.8)
+    both = Fields([inst, inst], "f32")
+    both.set_design(des, 0)
+    both.set_design(des2, 1)
+    Fb, gb = both.adjoint_gradient([obj, obj], N_STEPS, checkpoint_every=60)
+    for q, d in enumerate((des, des2)):
+        one = Fields(inst, "f32")
+        one.set_design(d)
+        F1, g1 = one.adjoint_gradient(obj, N_STEPS, checkpoint_every=60)
+        assert Fb[q] == F1[0]
+        np.testing.assert_array_equal(gb[q], g1[0])
+
+
+def test_design_region_requires_the_split_schedule(lib):
+    inst, des, obj = setup()
+    f = Fields(inst, "f32")
+    f.set_design(des)
+    with pytest.raises(_abi.SJError):
+        f.set_schedule("fused")
+    f.set_design(None)
+    f.set_schedule("fused")
+
+
+def test_torch_autograd_binding(lib):
+    torch = pytest.importorskip("torch")
+    from sim_juncs_gb300.autograd import GapFieldObjective
+    inst, des, obj = setup()
+    f = Fields(inst, "f32")
+    eps = torch.tensor(des.eps, dtype=torch.float64, requires_grad=True)
+    F = GapFieldObjective.apply(eps, f, des.lo, obj, N_STEPS, 60)
+    F.backward()
+    g = Fields(inst, "f32")
+    g.set_design(des)
+    F2, g2 = g.adjoint_gradient(obj, N_STEPS, checkpoint_every=60)
+    assert float(F.detach()) == F2[0]
+    np.testing.assert_allclose(eps.grad.numpy(), g2[0], rtol=1e-6, atol=0)
