@@ -358,6 +358,8 @@ int sj_set_design(sj_sim* sim, int32_t inst, const sj_design_desc* design);
 /* objectives[n_instances]; d_obj_d_eps holds every instance's design voxels */
 int sj_adjoint_gradient(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_steps,
                         int32_t checkpoint_every, double* d_obj_d_eps, size_t cap, double* obj);
+/* the forward half alone: F per instance after n_steps from rest */
+int sj_objective(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_steps, double* obj);
 
 /* ---------------------------------------------------------------- rasteriser */
 /* cgs_material_function::in_bound per E-component Yee point, on the device:

@@ -133,3 +133,19 @@ def sweep_instances(per_size=32, sizes=((96, 30.0), (128, 40.0), (192, 60.0)), s
             out.append(junction_instance(n=n, res=res, phase=cep, amplitude=amp,
                                          probe_components=("Ez",), dft=False))
     return out
+
+
+def adjoint_case(n=160, res=30.0, seed=1, design_um=(0.6, 0.6, 0.1), patch=5):
+    """c3: the Au box-pair junction at n^3 (30 px/um: 160^3), a design region
+    of design_um centred in the gap with eps ~ U[1, 4] from `seed`, and
+    |E(fcen)|^2 summed over a patch x patch gap patch in the junction's
+    mid plane.  Returns (instance, design, objective)."""
+    from .spec import Design, Objective
+    inst = junction_instance(n=n, res=res, probe_components=("Ex",), dft=False)
+    dx = 1.0 / res
+    nd = [max(1, int(round(u / dx))) for u in design_um]
+    c = n // 2
+    lo = (c - nd[0] // 2, c - nd[1] // 2, c - nd[2] // 2)
+    eps = np.random.default_rng(seed).uniform(1.0, 4.0, size=(nd[2], nd[1], nd[0]))
+    cells = np.array([[c - patch // 2 + a, c - patch // 2 + b, c] for b in range(patch) for a in range(patch)])
+    return inst, Design(lo, eps), Objective(cells, frequency=1 / 0.7, comps=(0, 1, 2))

@@ -1132,7 +1132,7 @@ void set_dev_step(sj_sim* sim, long long step) {
 
 template <typename real>
 void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long long K, double* grad, size_t cap,
-               double* objv) {
+               double* objv, bool backward = true) {
     auto& hv = hostv<real>(sim);
     auto& dv = devv<real>(sim);
     const int ni = sim->n_inst;
@@ -1151,7 +1151,9 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
         }
         total_d += (long long)hv[q].des_eps.size();
     }
-    if (total_d > 0 && (!grad || (size_t)total_d > cap)) fail(SJ_E_RANGE, "d_obj_d_eps too small for the design voxels");
+    if (backward && total_d > 0 && (!grad || (size_t)total_d > cap))
+        fail(SJ_E_RANGE, "d_obj_d_eps too small for the design voxels");
+    if (!backward) K = N;  // the final state is the only one kept
     sim->schedule = SJ_SCHED_SPLIT;
     sim->drop_graphs();
     ensure_capacity<real>(sim, N);
@@ -1236,6 +1238,11 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
             for (const double2& v : D) F += v.x * v.x + v.y * v.y;
         }
         objv[q] = F;
+    }
+    if (!backward) {
+        sim->t = N;  // the device counter advanced with the steps
+        for (void* p : temps) sim->dfree(p);
+        return;
     }
     // ---- adjoint buffers
     std::vector<AdjDev<real>> A(ni);
@@ -1419,6 +1426,16 @@ int sj_set_design(sj_sim* sim, int32_t inst, const sj_design_desc* design) {
         set_design_t<double>(sim, inst, design);
     else
         set_design_t<float>(sim, inst, design);
+    SJ_CATCH(sim)
+}
+
+int sj_objective(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_steps, double* obj) {
+    if (!sim) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        adjoint_t<double>(sim, objectives, n_steps, n_steps, nullptr, 0, obj, false);
+    else
+        adjoint_t<float>(sim, objectives, n_steps, n_steps, nullptr, 0, obj, false);
     SJ_CATCH(sim)
 }
 

@@ -174,6 +174,22 @@ class Fields:
             off += n
         return F, out
 
+    def objective(self, objectives, n_steps):
+        """F per instance after n_steps from rest (the forward half of
+        adjoint_gradient)."""
+        if not isinstance(objectives, (list, tuple)):
+            objectives = [objectives]
+        assert len(objectives) == self.n_instances
+        arr = (_abi.ObjectiveDesc * self.n_instances)()
+        keep = []
+        for q, ob in enumerate(objectives):
+            o, k = ob.to_c()
+            arr[q] = o
+            keep.append(k)
+        F = np.zeros(self.n_instances, dtype=np.float64)
+        self._ck(self.lib.sj_objective(self.handle, arr, int(n_steps), F.ctypes.data_as(C.POINTER(C.c_double))))
+        return F
+
     def schedule_name(self):
         """The schedule in use: "fused", "split" or "tma"."""
         return {_abi.SCHED_FUSED: "fused", _abi.SCHED_SPLIT: "split", _abi.SCHED_TMA: "tma"}[

@@ -71,6 +71,18 @@ def test_state_after_adjoint_equals_plain_stepping(lib):
     np.testing.assert_array_equal(a.monitors(), b.monitors())
 
 
+def test_objective_is_the_forward_half(lib):
+    inst, des, obj = setup()
+    f = Fields(inst, "f64")
+    f.set_design(des)
+    F, _ = f.adjoint_gradient(obj, N_STEPS, checkpoint_every=80)
+    f.synchronize()  # host and device step counters agree
+    F2 = f.objective(obj, N_STEPS)
+    f.synchronize()
+    assert f.steps_done == N_STEPS
+    assert F2[0] == F[0]
+
+
 def test_batched_designs_equal_separate_runs(lib):
     inst, des, obj = setup()
     des2 = Design(des.lo, des.eps[::-1, ::-1, :].copy() * 0.8)
