@@ -306,6 +306,14 @@ int32_t sj_launches_per_step(const sj_sim* sim);
 int sj_read_monitors(sj_sim* sim, int32_t inst, double* out, size_t cap);
 /* running DFT sums: out[dft_probe][freq][re, im] */
 int sj_read_dft(sj_sim* sim, int32_t inst, double* out, size_t cap);
+/* The spectrum save_field_times writes per monitor (src/disp.cpp:804, the
+   fft of src/data_utils.cpp:413-427), computed on the device from the
+   samples so far: of N samples the first N' = 2^floor(log2 N) are used and
+   F_k = sum_{m<N'} x_m e^{-i 2 pi m k / N} for k = -N'/2 .. N'/2-1, stored
+   at index k mod N'.  out[monitor][N'][re, im]; sj_monitor_spectrum_length
+   gives N'. */
+int64_t sj_monitor_spectrum_length(const sj_sim* sim, int32_t inst);
+int sj_monitor_spectrum(sj_sim* sim, int32_t inst, double* out, size_t cap);
 /* full component array converted to FP64 (dump_raw, src/disp.cpp:732-737) */
 int sj_read_field(sj_sim* sim, int32_t inst, int32_t component, double* out, size_t cap);
 /* overwrite one component (initial conditions / checkpoint restore) */

@@ -12,8 +12,9 @@
 //     and here the standard explicit-instantiation idiom reads them;
 //   * restate parse_susceptibilities (src/disp.cpp:418-454), which lives in
 //     meep-dependent code, on the root's "susceptibilities" metadata.
-// It also exposes composite_object::in (src/cgs.cpp:431-456) itself, the
-// answer the golden vectors record.
+// It also exposes composite_object::in (src/cgs.cpp:431-456) itself and the
+// reference's fft (src/data_utils.cpp:413-427, the transform save_field_times
+// applies to each monitor series), the answers the golden vectors record.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -21,6 +22,7 @@
 
 #include "cgs.hpp"
 #include "cgs_read.hpp"
+#include "data_utils.hpp"
 #include "../include/sj.h"
 
 namespace {
@@ -243,6 +245,26 @@ int sjref_root_poles(int h, int r, double* omega_0, double* gamma, double* sigma
         ++n;
     }
     return n;
+}
+
+// fft of the series re + i im (n points): writes the result (its length is
+// returned, at most cap complex values) as out[k][re, im].
+int64_t sjref_fft(const double* re, const double* im, int64_t n, double* out, int64_t cap) {
+    data_arr dat;
+    make_data_arr_zeros(&dat, (_ulong)n);
+    for (int64_t q = 0; q < n; ++q) {
+        dat.buf[q].re = re[q];
+        dat.buf[q].im = im[q];
+    }
+    data_arr r = fft(dat);
+    const int64_t m = (int64_t)r.size;
+    for (int64_t k = 0; k < m && k < cap; ++k) {
+        out[2 * k] = r.buf[k].re;
+        out[2 * k + 1] = r.buf[k].im;
+    }
+    cleanup_data_arr(&r);
+    cleanup_data_arr(&dat);
+    return m;
 }
 
 // composite_object::in of root r at n points (xyz interleaved).

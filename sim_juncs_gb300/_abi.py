@@ -134,6 +134,8 @@ SIGNATURES = {
     "sj_set_design": (C.c_int, [_P, C.c_int32, C.POINTER(DesignDesc)]),
     "sj_adjoint_gradient": (C.c_int, [_P, C.POINTER(ObjectiveDesc), C.c_int64, C.c_int32, _D, C.c_size_t, _D]),
     "sj_objective": (C.c_int, [_P, C.POINTER(ObjectiveDesc), C.c_int64, _D]),
+    "sj_monitor_spectrum_length": (C.c_int64, [_P, C.c_int32]),
+    "sj_monitor_spectrum": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_monitors": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_dft": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

@@ -1584,6 +1584,35 @@ int64_t sj_n_samples(const sj_sim* sim, int32_t inst) {
     return (sim->t + ss - 1) / ss;
 }
 
+int64_t sj_monitor_spectrum_length(const sj_sim* sim, int32_t inst) {
+    const int64_t n = sj_n_samples(sim, inst);
+    if (n < 1) return n < 0 ? -1 : 0;
+    // as the reference computes it: (unsigned long)(log(N) / log(2))
+    const unsigned long l2 = (unsigned long)(std::log((double)n) / std::log(2.0));
+    return (int64_t)1 << l2;
+}
+
+int sj_monitor_spectrum(sj_sim* sim, int32_t inst, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    check_status(sim);
+    const int nm = sim->precision == SJ_F64 ? sim->hi64[inst].n_mon : sim->hi32[inst].n_mon;
+    const double* dm = sim->precision == SJ_F64 ? sim->hi64[inst].d_mon : sim->hi32[inst].d_mon;
+    const long long n = sj_n_samples(sim, inst), np = sj_monitor_spectrum_length(sim, inst);
+    if ((size_t)nm * np * 2 > cap) fail(SJ_E_RANGE, "out too small: n_monitors * length * 2 doubles");
+    if (nm > 0 && np > 0) {
+        double* d_out = (double*)sim->dalloc((size_t)nm * np * 2 * sizeof(double), false);
+        cudaError_t e = launch_spectrum(dm, nm, n, np, d_out, sim->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sim->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(out, d_out, (size_t)nm * np * 2 * sizeof(double), cudaMemcpyDeviceToHost);
+        sim->dfree(d_out);
+        ck(e, "monitor spectrum");
+        sim->d2h += (long long)nm * np * 2 * sizeof(double);
+    }
+    SJ_CATCH(sim)
+}
+
 int sj_read_monitors(sj_sim* sim, int32_t inst, double* out, size_t cap) {
     if (!sim || inst < 0 || inst >= sim->n_inst) return SJ_E_INVALID;
     SJ_TRY(sim)

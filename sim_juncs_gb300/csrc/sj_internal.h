@@ -199,6 +199,10 @@ template <typename real>
 cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells, int n_cells, int comp_mask,
                              double freq, double2* d_D, long long n, bool sample, real* const* eb, cudaStream_t s);
 
+// Monitor spectra (sj_spectrum.cu): out[monitor][np][re, im] from the
+// monitor buffer mon[sample][n_mon] (n samples, np = 2^floor(log2 n)).
+cudaError_t launch_spectrum(const double* d_mon, int n_mon, long long n, long long np, double* d_out, cudaStream_t s);
+
 // Launch helpers implemented in sj_raster.cu.
 cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_start,
                              int n_regions, int nx, int ny, int nz, double dx,

@@ -212,6 +212,16 @@ class Fields:
                                            out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out
 
+    def monitor_spectrum(self, inst=0):
+        """The per-monitor spectrum save_field_times writes: [monitor][N']
+        complex, N' = 2^floor(log2 samples)."""
+        nm = self.instances[inst].n_monitors
+        npts = int(self.lib.sj_monitor_spectrum_length(self.handle, inst))
+        out = np.zeros((nm, max(npts, 0), 2), dtype=np.float64)
+        self._ck(self.lib.sj_monitor_spectrum(self.handle, inst, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                              out.size))
+        return out[..., 0] + 1j * out[..., 1]
+
     def dft(self, inst=0):
         """Running DFT sums: complex [dft_probe][freq]."""
         nd = self.instances[inst].n_dft

@@ -20,6 +20,9 @@ composite of it, the file records:
   * for tests/test.geom, in() at the six points src/main_test.cpp:1555-1564
     checks.
 
+fft_reference.json holds the reference's fft (src/data_utils.cpp:413-427) of
+seeded series of several lengths.
+
 The parser executes snapshot(...) statements (it draws an image file), so
 each file is parsed from a copy without them, written under the repository's
 git-ignored _work/ folder; snapshots do not change the geometry.  The
@@ -133,6 +136,31 @@ def record(lib, h, name, origin, dx, ambient):
     return {"grid": {"n": GRID_N, "origin": list(origin), "dx": dx}, "ambient_eps": ambient, "roots": roots}
 
 
+FFT_OUT = os.path.join(HERE, "fft_reference.json")
+FFT_SIZES = (1, 2, 3, 7, 8, 16, 33, 64, 100, 128, 257, 1000)
+
+
+def write_fft(lib):
+    """The reference's fft (src/data_utils.cpp:413-427) on seeded real and
+    complex series of several lengths, powers of two included."""
+    lib.sjref_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double),
+                              C.c_int64]
+    lib.sjref_fft.restype = C.c_int64
+    rng = np.random.default_rng(7)
+    cases = []
+    for n in FFT_SIZES:
+        for cplx in (False, True):
+            re = rng.standard_normal(n)
+            im = rng.standard_normal(n) if cplx else np.zeros(n)
+            out = np.zeros(2 * n)
+            m = lib.sjref_fft(re.ctypes.data_as(C.POINTER(C.c_double)), im.ctypes.data_as(C.POINTER(C.c_double)), n,
+                              out.ctypes.data_as(C.POINTER(C.c_double)), n)
+            cases.append({"n": n, "re": re.tolist(), "im": im.tolist(), "out_len": int(m),
+                          "out": out[:2 * m].tolist()})
+    with open(FFT_OUT, "w") as fh:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, fh)
+
+
 def main(ref_root):
     lib = load_lib()
     os.makedirs(SCRATCH, exist_ok=True)
@@ -168,6 +196,7 @@ def main(ref_root):
         out["files"][name] = entry
     with open(OUT, "w") as fh:
         json.dump(out, fh, indent=1)
+    write_fft(lib)
     for name, e in out["files"].items():
         print(name, [(len(r["nodes"]), r["n_inside"], r["eps"], len(r["poles"])) for r in e["roots"]])
 

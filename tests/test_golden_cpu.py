@@ -143,3 +143,31 @@ def test_gaussian_source_timing():
     s2 = Source(_abi.EX, 1.0, 2.0, 0.0, 2 * 5 * 2.0, (0, 0, 0), (1, 1, 0))
     assert 2 * np.pi * s2.frequency == pytest.approx(6.283185307)
     assert 1 / s2.width == pytest.approx(0.5)
+
+
+def reference_spectrum(x):
+    """Restatement of the reference's fft (src/data_utils.cpp:413-427): the
+    first N' = 2^floor(log2 N) samples, phase step 2 pi / N, bins
+    k = -N'/2 .. N'/2 - 1 stored at k mod N'."""
+    import math
+    x = np.asarray(x, dtype=np.complex128)
+    n = len(x)
+    npow = 1 << int(math.log(n) / math.log(2))
+    out = np.zeros(npow, dtype=np.complex128)
+    if npow > 1:
+        k = np.arange(-npow // 2, npow // 2)
+        m = np.arange(npow)
+        out[k % npow] = (x[:npow][None, :] * np.exp(-2j * np.pi * np.outer(k, m) / n)).sum(axis=1)
+    return out
+
+
+def test_spectrum_restatement_matches_reference_fft():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "fft_reference.json")) as fh:
+        cases = json.load(fh)["cases"]
+    assert {c["n"] for c in cases} >= {1, 8, 64, 100, 1000}
+    for c in cases:
+        want = np.array(c["out"][0::2]) + 1j * np.array(c["out"][1::2])
+        got = reference_spectrum(np.array(c["re"]) + 1j * np.array(c["im"]))
+        assert len(got) == c["out_len"], c["n"]
+        scale = max(1.0, float(np.max(np.abs(want))))
+        assert float(np.max(np.abs(got - want))) <= 1e-12 * scale, c["n"]

@@ -22,3 +22,20 @@ def test_device_rasterizer_matches_reference_in(lib, name):
     for r, root in enumerate(e["roots"]):
         want = unpack(root["inside_bits"], 3 * n ** 3).reshape(3, n, n, n)
         np.testing.assert_array_equal((masks >> r) & 1, want)
+
+
+def test_device_monitor_spectrum(lib):
+    # the spectrum save_field_times writes, computed on the device, against
+    # the restatement pinned to the reference's fft
+    from sim_juncs_gb300.configs import junction_instance
+    from sim_juncs_gb300.fields import Fields
+    from test_golden_cpu import reference_spectrum
+    f = Fields(junction_instance(), "f32")
+    for steps in (7 * 20, 2000):  # 7 samples (4 bins), 100 samples (64 bins)
+        f.step(steps - f.steps_done)
+        mon = f.monitors()
+        spec = f.monitor_spectrum()
+        assert spec.shape == (mon.shape[0], len(reference_spectrum(mon[0])))
+        for m in range(mon.shape[0]):
+            want = reference_spectrum(mon[m])
+            assert float(np.max(np.abs(spec[m] - want))) <= 1e-12 * max(1e-300, float(np.max(np.abs(want))))
