@@ -54,6 +54,9 @@ constexpr int LMAXF = 256;
 #ifndef SJ_LEAN_PLAIN_MINB
 #define SJ_LEAN_PLAIN_MINB 5
 #endif
+#ifndef SJ_LEAN_PAIR_PLAIN_MINB
+#define SJ_LEAN_PAIR_PLAIN_MINB 8
+#endif
 #ifndef SJ_LEAN_SLAB_MINB
 #define SJ_LEAN_SLAB_MINB 5
 #endif
@@ -65,6 +68,10 @@ constexpr int LMAXF = 256;
 #endif
 template <typename real>
 constexpr int plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PLAIN_MINB : 3; }
+// the two-column plain kernel's 128-thread blocks
+template <typename real>
+constexpr int pair_plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PAIR_PLAIN_MINB : 4; }
+
 template <typename real>
 constexpr int slab_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB_MINB : 2; }
 template <typename real>
@@ -121,6 +128,13 @@ __host__ __device__ inline bool tile_has_hsource(const InstDev<real>& I, int i0,
             return true;
     }
     return false;
+}
+
+// Does the tile's footprint or its z+1 plane reach a face of the grid?
+template <typename real>
+__host__ __device__ inline bool tile_edge(const InstDev<real>& I, int tx, int ty, int tz, int zb) {
+    const int i0 = tx * LX, j0 = ty * LY, z1 = imin(I.nz, (tz + 1) * zb);
+    return !(i0 > 0 && i0 + LX < I.nx && j0 > 0 && j0 + LY < I.ny && z1 < I.nz);
 }
 
 // ------------------------------------------------------------- plain tiles
@@ -197,6 +211,31 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
         eym_c = eym_n;
     }
 }
+
+// Vector pairs for the two-column tile body (tile_pair, below).
+template <typename real>
+struct Pair;
+template <>
+struct Pair<float> {
+    using T = float2;
+};
+template <>
+struct Pair<double> {
+    using T = double2;
+};
+template <typename real>
+__device__ __forceinline__ typename Pair<real>::T ld2(const real* p, unsigned o) {
+    return __ldg(reinterpret_cast<const typename Pair<real>::T*>(p + o));
+}
+template <typename real>
+__device__ __forceinline__ void st2(real* p, unsigned o, real a, real b) {
+    typename Pair<real>::T v;
+    v.x = a;
+    v.y = b;
+    *reinterpret_cast<typename Pair<real>::T*>(p + o) = v;
+}
+
+constexpr unsigned FULL = 0xffffffffu;
 
 // ------------------------------------------------------- slab / general tiles
 // dt J of every source of component `comp` covering (i, j, k) at step n
@@ -483,6 +522,268 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
     }
 }
 
+template <typename real>
+__device__ __forceinline__ typename Pair<real>::T ld2z(const real* p, unsigned o, bool ok) {
+    typename Pair<real>::T v;
+    if (ok) return ld2(p, o);
+    v.x = v.y = real(0);
+    return v;
+}
+
+// Two columns per thread (instances whose nx is a multiple of 32, so every
+// pair of a row exists): a half-warp of 16 lanes covers one 32-column row
+// (lane l: columns 2l and 2l+1) and a block of 4 warps the tile's 8 rows.
+// Fields move as pairs (float2 / double2); the H at x-1 that the E update
+// needs comes from the neighbouring lane by shuffle instead of being
+// recomputed, lane 0 recomputes it for the column left of the tile and lane
+// 15 loads the E right of it.  CPML on the axes in MASK (MASK = 0: plain
+// tiles).  Each voxel evaluates tile_block's formulas through the same
+// pml_term calls in the same order, so both bodies give the same bits.
+// Rows beyond ny (EDGE only) run with a clamped row and store nothing, so
+// that every lane reaches the shuffles.
+template <typename real, int ZB, int MASK, bool EDGE>
+__device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty, int tz, bool dry) {
+    using V2 = typename Pair<real>::T;
+    constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
+    const int lane = threadIdx.x & 15, half = threadIdx.x >> 4;
+    const int i = tx * LX + 2 * lane;
+    const int jr = ty * LY + threadIdx.y * 2 + half;
+    const bool act = !EDGE || jr < I.ny;
+    const int j = act ? jr : I.ny - 1;
+    const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
+    const int nx = I.nx, ny = I.ny, nz = I.nz;
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
+    const real* eX = I.F[0][0];
+    const real* eY = I.F[0][1];
+    const real* eZ = I.F[0][2];
+    const real* hX = I.F[0][3];
+    const real* hY = I.F[0][4];
+    const real* hZ = I.F[0][5];
+    real* oEX = I.F[1][0];
+    real* oEY = I.F[1][1];
+    real* oEZ = I.F[1][2];
+    real* oHX = I.F[1][3];
+    real* oHY = I.F[1][4];
+    real* oHZ = I.F[1][5];
+    const real* hiX = SX ? I.psiH[0][0] : nullptr;
+    const real* hiY = SY ? I.psiH[0][1] : nullptr;
+    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
+    real* hoX = SX ? I.psiH[1][0] : nullptr;
+    real* hoY = SY ? I.psiH[1][1] : nullptr;
+    real* hoZ = SZ ? I.psiH[1][2] : nullptr;
+    real* peX = SX ? I.psiE[0] : nullptr;
+    real* peY = SY ? I.psiE[1] : nullptr;
+    real* peZ = SZ ? I.psiE[2] : nullptr;
+    const real S = I.S;
+
+    const bool xm = !EDGE || i > 0, xp1 = !EDGE || i + 2 < nx;
+    const bool ym = !EDGE || j > 0, yp = !EDGE || j + 1 < ny;
+    const bool hm = lane == 0 && xm, hp = lane == 15 && xp1;
+    // slab membership: both columns, the halo column left of the tile, the row and the row below
+    const bool xo0 = SX && in_slab(I, 0, i), xo1 = SX && in_slab(I, 0, i + 1);
+    const bool xoh = SX && hm && in_slab(I, 0, i - 1);
+    const bool yo = SY && in_slab(I, 1, j), yo_m = SY && ym && in_slab(I, 1, j - 1);
+    real bxi0 = 1, cxi0 = 0, bxh0 = 1, cxh0 = 0, bxi1 = 1, cxi1 = 0, bxh1 = 1, cxh1 = 0, bxhh = 1, cxhh = 0;
+    real byi = 1, cyi = 0, byh = 1, cyh = 0, byhm = 1, cyhm = 0;
+    if (SX) {
+        const real* pr = I.prof[0];
+        if (xo0) bxi0 = ldg(pr, i), cxi0 = ldg(pr, nx + i), bxh0 = ldg(pr, 2 * nx + i), cxh0 = ldg(pr, 3 * nx + i);
+        if (xo1)
+            bxi1 = ldg(pr, i + 1), cxi1 = ldg(pr, nx + i + 1), bxh1 = ldg(pr, 2 * nx + i + 1),
+            cxh1 = ldg(pr, 3 * nx + i + 1);
+        if (xoh) bxhh = ldg(pr, 2 * nx + i - 1), cxhh = ldg(pr, 3 * nx + i - 1);
+    }
+    if (SY) {
+        const real* pr = I.prof[1];
+        if (yo) byi = ldg(pr, j), cyi = ldg(pr, ny + j), byh = ldg(pr, 2 * ny + j), cyh = ldg(pr, 3 * ny + j);
+        if (yo_m) byhm = ldg(pr, 2 * ny + j - 1), cyhm = ldg(pr, 3 * ny + j - 1);
+    }
+
+    int k = z0 > 0 ? z0 - 1 : 0;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+    V2 ex_c = ld2(eX, o), ey_c = ld2(eY, o), eym_c = ld2z(eY, o - px, ym);
+    real exm_c = hm ? ldg(eX, o - 1) : real(0);
+    V2 hxp, hyp;
+    hxp.x = hxp.y = hyp.x = hyp.y = real(0);
+    const unsigned orow = o - 2 * lane;  // row start of this half-warp at plane k
+    const int k0 = k;
+    const int i0 = tx * LX;
+    const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
+    for (; k < z1; ++k, o += plane) {
+        const bool kp = !EDGE || k + 1 < nz;
+        const bool store = k >= z0;
+        const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
+        if (LEAN_PF > 0 && lane == 0 && act && k + 1 + LEAN_PF < nz && k + LEAN_PF < z1) {
+            const int kq = k + 1 + LEAN_PF;
+            const unsigned r = orow + (unsigned)(kq - k0) * plane;
+            prefetch_row(eX + r);
+            prefetch_row(eY + r);
+            prefetch_row(eZ + r);
+            prefetch_row(hX + r);
+            prefetch_row(hY + r);
+            prefetch_row(hZ + r);
+            prefetch_row(I.combo + r);
+            if (xt) {
+                prefetch_row(hiX + r), prefetch_row(hiX + vol + r);
+                prefetch_row(peX + r), prefetch_row(peX + vol + r);
+            }
+            if (SY && yo) {
+                prefetch_row(hiY + r), prefetch_row(hiY + vol + r);
+                prefetch_row(peY + r), prefetch_row(peY + vol + r);
+            }
+            if (SZ && (kq < I.pl[2] || kq >= nz - I.ph[2])) {
+                prefetch_row(hiZ + r), prefetch_row(hiZ + vol + r);
+                prefetch_row(peZ + r), prefetch_row(peZ + vol + r);
+            }
+        }
+        real bzi = 1, czi = 0, bzh = 1, czh = 0;
+        if (zo) {
+            const real* pr = I.prof[2];
+            bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
+        }
+        const V2 ex_n = ld2z(eX, o + plane, kp), ey_n = ld2z(eY, o + plane, kp);
+        const V2 eym_n = ld2z(eY, o + plane - px, kp && ym);
+        const real exm_n = (hm && kp) ? ldg(eX, o + plane - 1) : real(0);
+        const V2 ez = ld2(eZ, o), ez_yp = ld2z(eZ, o + px, yp), ex_yp = ld2z(eX, o + px, yp);
+        real ez_x2 = __shfl_down_sync(FULL, ez.x, 1, 16), ey_x2 = __shfl_down_sync(FULL, ey_c.x, 1, 16);
+        const real ez_x2l = hp ? ldg(eZ, o + 2) : real(0), ey_x2l = hp ? ldg(eY, o + 2) : real(0);
+        if (lane == 15) ez_x2 = ez_x2l, ey_x2 = ey_x2l;
+        const V2 h_x = ld2(hX, o), h_y = ld2(hY, o), h_z = ld2(hZ, o);
+        const bool sp = store && !dry && act;
+
+        V2 hx, hy, hz;
+        {
+            real d1 = ez_yp.x - ez.x, d2 = ey_n.x - ey_c.x, cv = d1 - d2;
+            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o, sp);
+            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o, sp);
+            hx.x = fma(-S, cv, h_x.x);
+            d1 = ez_yp.y - ez.y, d2 = ey_n.y - ey_c.y, cv = d1 - d2;
+            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o + 1, sp);
+            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o + 1, sp);
+            hx.y = fma(-S, cv, h_x.y);
+        }
+        {
+            real d1 = ex_n.x - ex_c.x, d2 = ez.y - ez.x, cv = d1 - d2;
+            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o, sp);
+            pml_term<SX, false, true>(cv, xo0, bxh0, cxh0, d2, hiX, hoX, o, sp);
+            hy.x = fma(-S, cv, h_y.x);
+            d1 = ex_n.y - ex_c.y, d2 = ez_x2 - ez.y, cv = d1 - d2;
+            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o + 1, sp);
+            pml_term<SX, false, true>(cv, xo1, bxh1, cxh1, d2, hiX, hoX, o + 1, sp);
+            hy.y = fma(-S, cv, h_y.y);
+        }
+        {
+            real d1 = ey_c.y - ey_c.x, d2 = ex_yp.x - ex_c.x, cv = d1 - d2;
+            pml_term<SX, true, true>(cv, xo0, bxh0, cxh0, d1, hiX + vol, hoX + vol, o, sp);
+            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o, sp);
+            hz.x = fma(-S, cv, h_z.x);
+            d1 = ey_x2 - ey_c.y, d2 = ex_yp.y - ex_c.y, cv = d1 - d2;
+            pml_term<SX, true, true>(cv, xo1, bxh1, cxh1, d1, hiX + vol, hoX + vol, o + 1, sp);
+            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o + 1, sp);
+            hz.y = fma(-S, cv, h_z.y);
+        }
+        if (store) {
+            // H at x-1 (Hy, Hz): the previous lane's second column; lane 0 recomputes it
+            real hy_m = __shfl_up_sync(FULL, hy.y, 1, 16), hz_m = __shfl_up_sync(FULL, hz.y, 1, 16);
+            {
+                const unsigned om = o - 1;
+                const real ez_m = hm ? ldg(eZ, om) : real(0), ey_m = hm ? ldg(eY, om) : real(0);
+                const real exyp_m = (hm && yp) ? ldg(eX, om + px) : real(0);
+                real hy_l = 0, hz_l = 0;
+                if (hm) {
+                    real d1 = exm_n - exm_c, d2 = ez.x - ez_m, cv = d1 - d2;
+                    pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, om, false);
+                    pml_term<SX, false, true>(cv, xoh, bxhh, cxhh, d2, hiX, hoX, om, false);
+                    hy_l = fma(-S, cv, ldg(hY, om));
+                    d1 = ey_c.x - ey_m, d2 = exyp_m - exm_c, cv = d1 - d2;
+                    pml_term<SX, true, true>(cv, xoh, bxhh, cxhh, d1, hiX + vol, hoX + vol, om, false);
+                    pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, om, false);
+                    hz_l = fma(-S, cv, ldg(hZ, om));
+                }
+                if (lane == 0) hy_m = hy_l, hz_m = hz_l;
+            }
+            // H at y-1 (Hx, Hz), recomputed
+            const unsigned oy = o - px;
+            const V2 ez_ym = ld2z(eZ, oy, ym), ex_ym = ld2z(eX, oy, ym);
+            real eym_x2 = __shfl_down_sync(FULL, eym_c.x, 1, 16);
+            const real eym_x2l = (hp && ym) ? ldg(eY, oy + 2) : real(0);
+            if (lane == 15) eym_x2 = eym_x2l;
+            const V2 hx_y = ld2z(hX, oy, ym), hz_y = ld2z(hZ, oy, ym);
+            V2 hx_ym, hz_ym;
+            hx_ym.x = hx_ym.y = hz_ym.x = hz_ym.y = real(0);
+            if (ym) {
+                real d1 = ez.x - ez_ym.x, d2 = eym_n.x - eym_c.x, cv = d1 - d2;
+                pml_term<SY, true, true>(cv, yo_m, byhm, cyhm, d1, hiY, hoY, oy, false);
+                pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, oy, false);
+                hx_ym.x = fma(-S, cv, hx_y.x);
+                d1 = ez.y - ez_ym.y, d2 = eym_n.y - eym_c.y, cv = d1 - d2;
+                pml_term<SY, true, true>(cv, yo_m, byhm, cyhm, d1, hiY, hoY, oy + 1, false);
+                pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, oy + 1, false);
+                hx_ym.y = fma(-S, cv, hx_y.y);
+                d1 = eym_c.y - eym_c.x, d2 = ex_c.x - ex_ym.x, cv = d1 - d2;
+                pml_term<SX, true, true>(cv, xo0, bxh0, cxh0, d1, hiX + vol, hoX + vol, oy, false);
+                pml_term<SY, false, true>(cv, yo_m, byhm, cyhm, d2, hiY + vol, hoY + vol, oy, false);
+                hz_ym.x = fma(-S, cv, hz_y.x);
+                d1 = eym_x2 - eym_c.y, d2 = ex_c.y - ex_ym.y, cv = d1 - d2;
+                pml_term<SX, true, true>(cv, xo1, bxh1, cxh1, d1, hiX + vol, hoX + vol, oy + 1, false);
+                pml_term<SY, false, true>(cv, yo_m, byhm, cyhm, d2, hiY + vol, hoY + vol, oy + 1, false);
+                hz_ym.y = fma(-S, cv, hz_y.y);
+            }
+            if (act) {
+                st2(oHX, o, hx.x, hx.y);
+                st2(oHY, o, hy.x, hy.y);
+                st2(oHZ, o, hz.x, hz.y);
+            }
+            const uchar2 cb = __ldg(reinterpret_cast<const uchar2*>(I.combo + o));
+            const real* c0 = I.coef + (int)cb.x * I.ncoef;
+            const real* c1 = I.coef + (int)cb.y * I.ncoef;
+            const bool si = !dry && act;
+            V2 ex, ey, ezn;
+            {
+                real d1 = hz.x - hz_ym.x, d2 = hy.x - hyp.x, cv = d1 - d2;
+                pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
+                pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
+                ex.x = e_new<0>(I, c0, ex_c.x, cv);
+                d1 = hz.y - hz_ym.y, d2 = hy.y - hyp.y, cv = d1 - d2;
+                pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o + 1, si);
+                pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o + 1, si);
+                ex.y = e_new<0>(I, c1, ex_c.y, cv);
+            }
+            {
+                real d1 = hx.x - hxp.x, d2 = hz.x - hz_m, cv = d1 - d2;
+                pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
+                pml_term<SX, false, false>(cv, xo0, bxi0, cxi0, d2, peX, peX, o, si);
+                ey.x = e_new<1>(I, c0, ey_c.x, cv);
+                d1 = hx.y - hxp.y, d2 = hz.y - hz.x, cv = d1 - d2;
+                pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o + 1, si);
+                pml_term<SX, false, false>(cv, xo1, bxi1, cxi1, d2, peX, peX, o + 1, si);
+                ey.y = e_new<1>(I, c1, ey_c.y, cv);
+            }
+            {
+                real d1 = hy.x - hy_m, d2 = hx.x - hx_ym.x, cv = d1 - d2;
+                pml_term<SX, true, false>(cv, xo0, bxi0, cxi0, d1, peX + vol, peX + vol, o, si);
+                pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
+                ezn.x = e_new<2>(I, c0, ez.x, cv);
+                d1 = hy.y - hy.x, d2 = hx.y - hx_ym.y, cv = d1 - d2;
+                pml_term<SX, true, false>(cv, xo1, bxi1, cxi1, d1, peX + vol, peX + vol, o + 1, si);
+                pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o + 1, si);
+                ezn.y = e_new<2>(I, c1, ez.y, cv);
+            }
+            if (act) {
+                st2(oEX, o, ex.x, ex.y);
+                st2(oEY, o, ey.x, ey.y);
+                st2(oEZ, o, ezn.x, ezn.y);
+            }
+        }
+        hxp = hx;
+        hyp = hy;
+        ex_c = ex_n;
+        ey_c = ey_n;
+        eym_c = eym_n;
+        exm_c = exm_n;
+    }
+}
+
 // Monitors (every save_span steps, before the step) and running DFT sums, read
 // from buffer `cur`, which no stepping block writes during the launch.
 template <typename real>
@@ -567,12 +868,6 @@ __device__ __forceinline__ void finish_block(unsigned step_blocks, int dry, DevS
 }
 
 // Plain tiles: no CPML slab, source or dispersive voxel in the footprint.
-// Does the tile's footprint or its z+1 plane reach a face of the grid?
-template <typename real>
-__device__ __forceinline__ bool tile_edge(const InstDev<real>& I, int tx, int ty, int tz, int zb) {
-    const int i0 = tx * LX, j0 = ty * LY, z1 = min(I.nz, (tz + 1) * zb);
-    return !(i0 > 0 && i0 + LX < I.nx && j0 > 0 && j0 + LY < I.ny && z1 < I.nz);
-}
 
 template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, plain_minb<real>())
@@ -622,6 +917,26 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
         tile_block_any<real, ZB, 6, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
     else
         tile_block_any<real, ZB, 7, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+}
+
+// Plain tiles with two columns per thread (instances whose nx is a multiple
+// of 32), 4 warps per tile.  (The CPML tile classes keep one column per
+// thread: their two-column bodies need too many registers for the occupancy
+// the kernels live on.)
+template <typename real, int ZB, int MASK>
+__device__ __forceinline__ void tile_pair_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry) {
+    if (tile_edge(I, tx, ty, tz, ZB))
+        tile_pair<real, ZB, MASK, true>(I, tx, ty, tz, dry);
+    else
+        tile_pair<real, ZB, MASK, false>(I, tx, ty, tz, dry);
+}
+
+template <typename real, int ZB>
+__global__ void __launch_bounds__(LX * LY / 2, pair_plain_minb<real>())
+k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    tile_pair_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0);
 }
 
 // General tiles (a source or dispersive voxel in the footprint), then the
@@ -728,9 +1043,9 @@ int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists) 
                 const int i0 = tx * LX, j0 = ty * LY, z0 = tz * zb, z1 = imin(I.nz, z0 + zb);
                 const int m = tile_slab_mask(I, i0, j0, z0, z1);
                 const int c = tile_has_hsource(I, i0, j0, z0, z1) ? LEAN_GENERAL
-                              : m == 0                           ? LEAN_PLAIN
-                              : (m == 1 || m == 2 || m == 4)     ? LEAN_SLAB
-                                                                 : LEAN_MULTI;
+                              : m == 0                      ? LEAN_PLAIN
+                              : (m == 1 || m == 2 || m == 4) ? LEAN_SLAB
+                                                             : LEAN_MULTI;
                 lists[c].push_back((unsigned)tx | ((unsigned)ty << 9) | ((unsigned)tz << 19) | ((unsigned)m << 29));
             }
     return 0;
@@ -806,7 +1121,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     long long gtotal = 0;
     for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
-    const dim3 block(LX, LY);
+    const dim3 block(LX, LY), half(LX, LY / 2);
     for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
         LeanTable<real> t;
         t.inst = h_insts[q];
@@ -818,6 +1133,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         t.step_blocks = (unsigned)gtotal;
         const LeanTiles& T = tiles[q];
         const long long gb = general_blocks(h_insts[q], T, q, dry);
+        const bool pairs = h_insts[q].nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
         cudaStream_t sc[LEAN_CLASSES];
         for (int c = 0; c < LEAN_CLASSES; ++c)
             sc[c] = fork ? ls.side[(q % LEAN_SETS) * LEAN_CLASSES + c] : ls.main;
@@ -830,7 +1146,8 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         t.tiles = T.list[LEAN_GENERAL], t.n_tiles = T.count[LEAN_GENERAL];                                   \
         if (gb) k_lean_general<real, Z><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st);                \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
-        if (t.n_tiles) k_lean_plain<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_PLAIN]>>>(t);          \
+        if (t.n_tiles && pairs) k_lean_plain2<real, Z><<<(unsigned)t.n_tiles, half, 0, sc[LEAN_PLAIN]>>>(t); \
+        if (t.n_tiles && !pairs) k_lean_plain<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_PLAIN]>>>(t); \
         break;
         switch (zb) {  // z-segment length
             SJ_ZB(8)
