@@ -149,3 +149,31 @@ def adjoint_case(n=160, res=30.0, seed=1, design_um=(0.6, 0.6, 0.1), patch=5):
     eps = np.random.default_rng(seed).uniform(1.0, 4.0, size=(nd[2], nd[1], nd[0]))
     cells = np.array([[c - patch // 2 + a, c - patch // 2 + b, c] for b in range(patch) for a in range(patch)])
     return inst, Design(lo, eps), Objective(cells, frequency=1 / 0.7, comps=(0, 1, 2))
+
+
+def inverse_design_case(index, n=192, res=30.0, design_um=(0.8, 0.8, 0.1), patch=5):
+    """c4 design `index`: the Au box pair of c0 (Drude + Lorentz Au) on a
+    quartz substrate (eps_inf 2.1 plus one Lorentz term, f0 = 10, gamma = 0,
+    sigma = 0.25) filling the cell below the boxes, at n^3 and `res` px/um
+    (192^3, 30 px/um); a design_um region in the gap with eps ~ U[1, 4]
+    from seed `index`; |E(fcen)|^2 over a patch x patch gap patch as the
+    objective.  Returns (instance, design, objective)."""
+    from .spec import Design, Objective
+    inst = junction_instance(n=n, res=res, probe_components=("Ex",), dft=False)
+    dx = 1.0 / res
+    L = n * dx
+    c = L / 2
+    gap, bx, by, bz = 0.2, 1.0, 0.5, 0.1
+    au = Union(Box((c - gap / 2 - bx, c - by / 2, c - bz / 2), (c - gap / 2, c + by / 2, c + bz / 2)),
+               Box((c + gap / 2, c - by / 2, c - bz / 2), (c + gap / 2 + bx, c + by / 2, c + bz / 2)))
+    substrate = Box((0.0, 0.0, 0.0), (L, L, c - bz / 2))
+    # the first root containing a point decides (Au over quartz)
+    inst.material = Scene([Region(au, eps=1.0, susceptibilities=list(AU)),
+                           Region(substrate, eps=2.1, susceptibilities=list(QUARTZ))],
+                          ambient_eps=1.0, combine=_abi.EPS_FIRST)
+    nd = [max(1, int(round(u / dx))) for u in design_um]
+    m = n // 2
+    lo = (m - nd[0] // 2, m - nd[1] // 2, m - nd[2] // 2)
+    eps = np.random.default_rng(index).uniform(1.0, 4.0, size=(nd[2], nd[1], nd[0]))
+    cells = np.array([[m - patch // 2 + a, m - patch // 2 + b, m] for b in range(patch) for a in range(patch)])
+    return inst, Design(lo, eps), Objective(cells, frequency=1 / 0.7, comps=(0, 1, 2))
