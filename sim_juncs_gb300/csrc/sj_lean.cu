@@ -82,18 +82,21 @@ constexpr int general_minb() { return sizeof(real) == 4 ? SJ_LEAN_GEN_MINB : 2; 
 // Reads of buffer `cur` (fields, H-side psi), profiles and material tables
 // go through the non-coherent path: nothing writes them during the step, and
 // the compiler may then move them ahead of the stores of the previous plane.
-// L2 prefetch distance (planes): lane 0 of each warp (one 32-column row of
-// a tile) asks the TMA unit to bring the row of plane k + LEAN_PF of every
-// array the step reads into L2, so the loads of that plane find it there.
+// L2 prefetch distance (planes): each warp (one 32-column row of a tile)
+// asks the TMA unit to bring the row of plane k + LEAN_PF of every array the
+// step reads into L2, one row per lane, so the loads of that plane find it
+// there.
 #ifndef SJ_LEAN_PF
 #define SJ_LEAN_PF 2
 #endif
 constexpr int LEAN_PF = SJ_LEAN_PF;
 
-// one 32-element row at p (16-byte aligned: rows start on 128-byte boundaries)
-template <typename T>
-__device__ __forceinline__ void prefetch_row(const T* p) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "n"(32 * sizeof(T)));
+// `bytes` at p into L2 when on: one predicated instruction, no branch (rows
+// are 16-byte aligned: they start on 128-byte boundaries of padded rows)
+__device__ __forceinline__ void prefetch_if(const void* p, unsigned bytes, bool on) {
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q cp.async.bulk.prefetch.L2.global [%0], %1;\n\t}" ::"l"(p),
+        "r"(bytes), "r"((unsigned)on));
 }
 
 // Element offsets within an instance are 32-bit (the host rejects grids
@@ -137,6 +140,45 @@ __host__ __device__ inline bool tile_edge(const InstDev<real>& I, int tx, int ty
     return !(i0 > 0 && i0 + LX < I.nx && j0 > 0 && j0 + LY < I.ny && z1 < I.nz);
 }
 
+// The rows a column march prefetches into L2, LEAN_PF planes ahead, spread
+// one row per lane (a single predicated instruction per warp and plane):
+// lanes 0-5 the six field components, 6 the combo bytes, 7-10 the two psi
+// slots of H and of E along x (tiles touching an x slab), 11-14 those along
+// y (rows in a y slab), 15-18 those along z (planes in a z slab).  A lane's
+// row is one word: the array's address (16-byte aligned) with bit 0 set for
+// a z psi row and bit 1 for a byte array; 0 = no row.  The word waits in a
+// shared-memory slot of the thread and is reloaded on every plane, so it
+// holds no register across the march.
+template <typename real, bool SX, bool SY, bool SZ>
+__device__ __forceinline__ unsigned long long lane_row(const InstDev<real>& I, int l, bool xt, bool yt) {
+    if (l < 6) return (unsigned long long)I.F[0][l];
+    if (l == 6) return (unsigned long long)I.combo | 2ull;
+    if (l < 19) {
+        const int a = (l - 7) >> 2, q = (l - 7) & 3;
+        if (a == 0 ? SX && xt : (a == 1 ? SY && yt : SZ)) {
+            const real* b = q < 2 ? I.psiH[0][a] : I.psiE[a];
+            return (unsigned long long)(b + ((q & 1) ? I.vol : 0)) | (a == 2 ? 1ull : 0ull);
+        }
+    }
+    return 0;
+}
+constexpr int LEAN_PF_SLOTS = 256;  // threads of the largest tile block
+// park the thread's row word; returns its slot
+__device__ __forceinline__ volatile unsigned long long* lane_row_park(unsigned long long w) {
+    __shared__ unsigned long long slots[LEAN_PF_SLOTS];
+    volatile unsigned long long* s = slots + threadIdx.y * blockDim.x + threadIdx.x;
+    *s = w;
+    return s;
+}
+// the parked row at element offset r when the plane qualifies (zq: plane
+// kq inside a z slab)
+template <typename real>
+__device__ __forceinline__ void prefetch_lane_row(volatile unsigned long long* slot, unsigned r, bool on, bool zq) {
+    const unsigned long long w = *slot;
+    const unsigned esz = (w & 2) ? 1u : (unsigned)sizeof(real);
+    prefetch_if((const char*)(w & ~3ull) + (size_t)r * esz, 32 * esz, on && w != 0 && (zq || !(w & 1)));
+}
+
 // ------------------------------------------------------------- plain tiles
 // EDGE = false: the tile's footprint and its z+1 plane stay inside the grid,
 // so no load needs a bounds predicate.
@@ -167,18 +209,13 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;
     const unsigned orow = o - threadIdx.x;  // row start of this warp at plane k
+    const int k0 = k;
+    volatile unsigned long long* lr = lane_row_park(lane_row<real, false, false, false>(I, threadIdx.x, false, false));
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < I.nz;
-        if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < I.nz && k + LEAN_PF < z1) {
-            const unsigned r = orow + (unsigned)(k - (z0 > 0 ? z0 - 1 : 0) + 1 + LEAN_PF) * plane;
-            prefetch_row(eX + r);
-            prefetch_row(eY + r);
-            prefetch_row(eZ + r);
-            prefetch_row(hX + r);
-            prefetch_row(hY + r);
-            prefetch_row(hZ + r);
-            prefetch_row(I.combo + r);
-        }
+        if (LEAN_PF > 0)
+            prefetch_lane_row<real>(lr, orow + (unsigned)(k + 1 + LEAN_PF - k0) * plane,
+                              k + 1 + LEAN_PF < I.nz && k + LEAN_PF < z1, false);
         const real ex_n = ldz(eX, o + plane, kp), ey_n = ldz(eY, o + plane, kp);
         const real exm_n = ldz(eX, o + plane - 1, kp && xm), eym_n = ldz(eY, o + plane - px, kp && ym);
         const real ez = ldg(eZ, o);
@@ -264,12 +301,12 @@ template <bool AX, bool ADD, bool NC, typename real>
 __device__ __forceinline__ void pml_term(real& cv, bool on, real b, real c, real d, const real* pin, real* pout,
                                          unsigned x, bool store) {
     if (!AX) return;
+    // branch-free: predicated load and store, the term folded in by select;
+    // outside the slab cv + (-0) and cv - (+0) leave cv, sign of zero included
     const real po = on ? (NC ? __ldg(pin + x) : pin[x]) : real(0);
     const real ps = fma(b, po, c * d);
-    if (on) {
-        if (store) pout[x] = ps;
-        cv = ADD ? cv + ps : cv - ps;
-    }
+    if (on && store) pout[x] = ps;
+    cv = ADD ? cv + (on ? ps : real(-0.0)) : cv - (on ? ps : real(0));
 }
 
 // H^{n+1/2} = fma(-S, curl, H^{n-1/2}) [- dt J]
@@ -377,32 +414,15 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
     // (the arrays exist only for axes with slabs)
     const int i0 = tx * LX;
     const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
+    volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, threadIdx.x, xt, yo));
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
-        if (LEAN_PF > 0 && threadIdx.x == 0 && k + 1 + LEAN_PF < nz && k + LEAN_PF < z1) {
+        if (LEAN_PF > 0) {
             const int kq = k + 1 + LEAN_PF;
-            const unsigned r = orow + (unsigned)(kq - k0) * plane;
-            prefetch_row(eX + r);
-            prefetch_row(eY + r);
-            prefetch_row(eZ + r);
-            prefetch_row(hX + r);
-            prefetch_row(hY + r);
-            prefetch_row(hZ + r);
-            prefetch_row(I.combo + r);
-            if (xt) {
-                prefetch_row(hiX + r), prefetch_row(hiX + vol + r);
-                prefetch_row(peX + r), prefetch_row(peX + vol + r);
-            }
-            if (SY && yo) {
-                prefetch_row(hiY + r), prefetch_row(hiY + vol + r);
-                prefetch_row(peY + r), prefetch_row(peY + vol + r);
-            }
-            if (SZ && (kq < I.pl[2] || kq >= nz - I.ph[2])) {
-                prefetch_row(hiZ + r), prefetch_row(hiZ + vol + r);
-                prefetch_row(peZ + r), prefetch_row(peZ + vol + r);
-            }
+            prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, kq < nz && k + LEAN_PF < z1,
+                              SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
         }
         real bzi = 1, czi = 0, bzh = 1, czh = 0;
         if (zo) {
@@ -609,32 +629,16 @@ __device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty
     const int k0 = k;
     const int i0 = tx * LX;
     const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
+    // a half-warp's 16 lanes take rows 0-15: the z psi rows (SZ) go without
+    volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, lane, xt, yo));
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
-        if (LEAN_PF > 0 && lane == 0 && act && k + 1 + LEAN_PF < nz && k + LEAN_PF < z1) {
+        if (LEAN_PF > 0) {
             const int kq = k + 1 + LEAN_PF;
-            const unsigned r = orow + (unsigned)(kq - k0) * plane;
-            prefetch_row(eX + r);
-            prefetch_row(eY + r);
-            prefetch_row(eZ + r);
-            prefetch_row(hX + r);
-            prefetch_row(hY + r);
-            prefetch_row(hZ + r);
-            prefetch_row(I.combo + r);
-            if (xt) {
-                prefetch_row(hiX + r), prefetch_row(hiX + vol + r);
-                prefetch_row(peX + r), prefetch_row(peX + vol + r);
-            }
-            if (SY && yo) {
-                prefetch_row(hiY + r), prefetch_row(hiY + vol + r);
-                prefetch_row(peY + r), prefetch_row(peY + vol + r);
-            }
-            if (SZ && (kq < I.pl[2] || kq >= nz - I.ph[2])) {
-                prefetch_row(hiZ + r), prefetch_row(hiZ + vol + r);
-                prefetch_row(peZ + r), prefetch_row(peZ + vol + r);
-            }
+            prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, act && kq < nz && k + LEAN_PF < z1,
+                              SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
         }
         real bzi = 1, czi = 0, bzh = 1, czh = 0;
         if (zo) {
