@@ -58,10 +58,10 @@ constexpr int LMAXF = 256;
 #define SJ_LEAN_PAIR_PLAIN_MINB 8
 #endif
 #ifndef SJ_LEAN_SLAB_MINB
-#define SJ_LEAN_SLAB_MINB 5
+#define SJ_LEAN_SLAB_MINB 4
 #endif
 #ifndef SJ_LEAN_MULTI_MINB
-#define SJ_LEAN_MULTI_MINB 4
+#define SJ_LEAN_MULTI_MINB 3
 #endif
 #ifndef SJ_LEAN_GEN_MINB
 #define SJ_LEAN_GEN_MINB 4
@@ -162,7 +162,7 @@ __device__ __forceinline__ unsigned long long lane_row(const InstDev<real>& I, i
     }
     return 0;
 }
-constexpr int LEAN_PF_SLOTS = 256;  // threads of the largest tile block
+constexpr int LEAN_PF_SLOTS = LX * (LY + 2);  // threads of the largest tile block
 // park the thread's row word; returns its slot
 __device__ __forceinline__ volatile unsigned long long* lane_row_park(unsigned long long w) {
     __shared__ unsigned long long slots[LEAN_PF_SLOTS];
@@ -542,6 +542,192 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
     }
 }
 
+// ------------------------------------------------------ shared-halo tiles
+// CPML tiles with the neighbour H passed on instead of recomputed.  A block
+// of LY + 2 warps: warps 0..LY-1 the tile's rows j0..j0+LY-1 (lane l:
+// column i0+l), warp LY the row j0-1 and warp LY+1 the column i0-1 (lanes
+// 0..LY-1: rows j0..j0+LY-1).  On every plane each warp updates H at its
+// own cells through the same pml_term / h_new calls tile_block uses (the
+// halo warps store nothing: the tiles that own those cells do), so the H
+// a neighbour hands over has the bits tile_block would recompute.  Hx and Hz
+// go to the row above through a double-buffered shared plane (one barrier
+// per plane), Hy and Hz at x-1 come from the lane on the left by shuffle,
+// and lane 0 takes them from the column warp.  Against tile_block this
+// drops four recomputed H components (with their E, H and psi loads) per
+// cell for two H-only warps per tile.  Cells outside the grid (EDGE) run
+// with clamped coordinates, store nothing and are never read, so that every
+// thread reaches every barrier and shuffle.
+constexpr int HALO_WARPS = 2;
+constexpr int HALO_THREADS = LX * (LY + HALO_WARPS);
+
+template <typename real>
+struct HaloPlane {
+    real hx[LY + 1][LX];  // Hx of rows j0-1 .. j0+LY-1 (index: row - j0 + 1)
+    real hz[LY + 1][LX];
+    real xy[LY];          // Hy, Hz of column i0-1, rows j0 .. j0+LY-1
+    real xz[LY];
+};
+
+template <typename real, int ZB, int MASK, bool EDGE>
+__device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
+                                          HaloPlane<real>* sh) {
+    constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
+    const int w = threadIdx.y, lane = threadIdx.x;
+    const bool own = w < LY, rowh = w == LY, colh = w == LY + 1;
+    const int nx = I.nx, ny = I.ny, nz = I.nz;
+    const int i0 = tx * LX, j0 = ty * LY;
+    const int z0 = tz * ZB, z1 = min(nz, z0 + ZB);
+    int i = colh ? i0 - 1 : i0 + lane;
+    int j = own ? j0 + w : (rowh ? j0 - 1 : j0 + min(lane, LY - 1));
+    // a cell of the grid whose results are used
+    const bool act = (!EDGE || (i >= 0 && j >= 0 && i < nx && j < ny)) && (!colh || lane < LY);
+    if (EDGE) i = imin(imax(i, 0), nx - 1), j = imin(imax(j, 0), ny - 1);
+
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
+    const real* eX = I.F[0][0];
+    const real* eY = I.F[0][1];
+    const real* eZ = I.F[0][2];
+    const real* hX = I.F[0][3];
+    const real* hY = I.F[0][4];
+    const real* hZ = I.F[0][5];
+    real* oEX = I.F[1][0];
+    real* oEY = I.F[1][1];
+    real* oEZ = I.F[1][2];
+    real* oHX = I.F[1][3];
+    real* oHY = I.F[1][4];
+    real* oHZ = I.F[1][5];
+    const real* hiX = SX ? I.psiH[0][0] : nullptr;
+    const real* hiY = SY ? I.psiH[0][1] : nullptr;
+    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
+    real* hoX = SX ? I.psiH[1][0] : nullptr;
+    real* hoY = SY ? I.psiH[1][1] : nullptr;
+    real* hoZ = SZ ? I.psiH[1][2] : nullptr;
+    real* peX = SX ? I.psiE[0] : nullptr;
+    real* peY = SY ? I.psiE[1] : nullptr;
+    real* peZ = SZ ? I.psiE[2] : nullptr;
+
+    const bool xp = !EDGE || i + 1 < nx, yp = !EDGE || j + 1 < ny;
+    // the neighbours at x-1 (lane 0: the column warp) and y-1 (row 0: the row warp) exist
+    const bool xm = !EDGE || i0 > 0, ym = !EDGE || j0 > 0;
+    const bool xo = SX && in_slab(I, 0, i), yo = SY && in_slab(I, 1, j);
+    real bxi = 1, cxi = 0, bxh = 1, cxh = 0, byi = 1, cyi = 0, byh = 1, cyh = 0;
+    if (SX && xo) {
+        const real* pr = I.prof[0];
+        bxi = ldg(pr, i), cxi = ldg(pr, nx + i), bxh = ldg(pr, 2 * nx + i), cxh = ldg(pr, 3 * nx + i);
+    }
+    if (SY && yo) {
+        const real* pr = I.prof[1];
+        byi = ldg(pr, j), cyi = ldg(pr, ny + j), byh = ldg(pr, 2 * ny + j), cyh = ldg(pr, 3 * ny + j);
+    }
+
+    int k = z0 > 0 ? z0 - 1 : 0;
+    const int k0 = k;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+    real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
+    real hxp = 0, hyp = 0;  // H^{n+1/2} of plane k-1 at the own cell
+    // row prefetch: the tile rows and the row below them (the column warp's
+    // cells are not a row)
+    const bool xt = SX && (imax(i0 - 1, 0) < I.pl[0] || imin(i0 + LX, nx) - 1 >= nx - I.ph[0]);
+    const unsigned orow = (unsigned)k * plane + (unsigned)j * px + (unsigned)i0;
+    volatile unsigned long long* lr =
+        lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, lane, xt, yo));
+    for (; k < z1; ++k, o += plane) {
+        const bool kp = !EDGE || k + 1 < nz;
+        const bool store = k >= z0;  // block-uniform
+        const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
+        if (LEAN_PF > 0) {
+            const int kq = k + 1 + LEAN_PF;
+            prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, kq < nz && k + LEAN_PF < z1,
+                                    SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
+        }
+        real bzi = 1, czi = 0, bzh = 1, czh = 0;
+        if (zo) {
+            const real* pr = I.prof[2];
+            bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
+        }
+        const real ex_n = ldz(eX, o + plane, kp), ey_n = ldz(eY, o + plane, kp);
+        const real ez = ldg(eZ, o);
+        const real ez_xp = ldz(eZ, o + 1, xp), ez_yp = ldz(eZ, o + px, yp);
+        const real ey_xp = ldz(eY, o + 1, xp), ex_yp = ldz(eX, o + px, yp);
+        const bool sp = store && !dry && own && act;
+
+        // H^{n+1/2} at the warp's cells
+        real hx, hy, hz;
+        {
+            const real d1 = ez_yp - ez, d2 = ey_n - ey_c;
+            real cv = d1 - d2;
+            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o, sp);
+            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o, sp);
+            hx = h_new<false>(I, 3, cv, ldg(hX, o), false, i, j, k, 0);
+        }
+        {
+            const real d1 = ex_n - ex_c, d2 = ez_xp - ez;
+            real cv = d1 - d2;
+            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o, sp);
+            pml_term<SX, false, true>(cv, xo, bxh, cxh, d2, hiX, hoX, o, sp);
+            hy = h_new<false>(I, 4, cv, ldg(hY, o), false, i, j, k, 0);
+        }
+        {
+            const real d1 = ey_xp - ey_c, d2 = ex_yp - ex_c;
+            real cv = d1 - d2;
+            pml_term<SX, true, true>(cv, xo, bxh, cxh, d1, hiX + vol, hoX + vol, o, sp);
+            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o, sp);
+            hz = h_new<false>(I, 5, cv, ldg(hZ, o), false, i, j, k, 0);
+        }
+        if (store) {
+            HaloPlane<real>& b = sh[k & 1];
+            if ((own && w < LY - 1) || rowh) {
+                b.hx[rowh ? 0 : w + 1][lane] = hx;
+                b.hz[rowh ? 0 : w + 1][lane] = hz;
+            }
+            if (colh && lane < LY) {
+                b.xy[lane] = hy;
+                b.xz[lane] = hz;
+            }
+            __syncthreads();
+            if (own) {
+                real hy_xm = __shfl_up_sync(FULL, hy, 1), hz_xm = __shfl_up_sync(FULL, hz, 1);
+                if (lane == 0) hy_xm = xm ? b.xy[w] : real(0), hz_xm = xm ? b.xz[w] : real(0);
+                const bool yn = ym || w > 0;
+                const real hx_ym = yn ? b.hx[w][lane] : real(0), hz_ym = yn ? b.hz[w][lane] : real(0);
+                if (act) {
+                    oHX[o] = hx;
+                    oHY[o] = hy;
+                    oHZ[o] = hz;
+                    // E^{n+1} at the own cell
+                    const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
+                    const bool si = !dry;
+                    {
+                        const real d1 = hz - hz_ym, d2 = hy - hyp;
+                        real cv = d1 - d2;
+                        pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
+                        pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
+                        oEX[o] = e_new<0>(I, cf, ex_c, cv);
+                    }
+                    {
+                        const real d1 = hx - hxp, d2 = hz - hz_xm;
+                        real cv = d1 - d2;
+                        pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
+                        pml_term<SX, false, false>(cv, xo, bxi, cxi, d2, peX, peX, o, si);
+                        oEY[o] = e_new<1>(I, cf, ey_c, cv);
+                    }
+                    {
+                        const real d1 = hy - hy_xm, d2 = hx - hx_ym;
+                        real cv = d1 - d2;
+                        pml_term<SX, true, false>(cv, xo, bxi, cxi, d1, peX + vol, peX + vol, o, si);
+                        pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
+                        oEZ[o] = e_new<2>(I, cf, ez, cv);
+                    }
+                }
+            }
+        }
+        hxp = hx;
+        hyp = hy;
+        ex_c = ex_n;
+        ey_c = ey_n;
+    }
+}
+
 template <typename real>
 __device__ __forceinline__ typename Pair<real>::T ld2z(const real* p, unsigned o, bool ok) {
     typename Pair<real>::T v;
@@ -893,34 +1079,47 @@ __device__ __forceinline__ void tile_block_any(const InstDev<real>& I, int tx, i
         tile_block<real, ZB, MASK, EXTRAS, false>(I, tx, ty, tz, n, dry);
 }
 
+// sh: the kernel's two shared planes (declared once per kernel, not per
+// instantiation of the body)
+template <typename real, int ZB, int MASK>
+__device__ __forceinline__ void tile_halo_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
+                                              HaloPlane<real>* sh) {
+    if (tile_edge(I, tx, ty, tz, ZB))
+        tile_halo<real, ZB, MASK, true>(I, tx, ty, tz, dry, sh);
+    else
+        tile_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh);
+}
+
 // Single-slab tiles: the footprint touches the slabs of exactly one axis.
 template <typename real, int ZB>
-__global__ void __launch_bounds__(LX * LY, slab_minb<real>())
+__global__ void __launch_bounds__(HALO_THREADS, slab_minb<real>())
 k_lean_slab(const __grid_constant__ LeanTable<real> tab) {
+    __shared__ HaloPlane<real> sh[2];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     if (m == 1)
-        tile_block_any<real, ZB, 1, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 1>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
     else if (m == 2)
-        tile_block_any<real, ZB, 2, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 2>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
     else
-        tile_block_any<real, ZB, 4, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 4>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
 }
 
 // Multi-slab tiles: the slabs of two or three axes (edges and corners).
 template <typename real, int ZB>
-__global__ void __launch_bounds__(LX * LY, multi_minb<real>())
+__global__ void __launch_bounds__(HALO_THREADS, multi_minb<real>())
 k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
+    __shared__ HaloPlane<real> sh[2];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     if (m == 3)
-        tile_block_any<real, ZB, 3, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 3>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
     else if (m == 5)
-        tile_block_any<real, ZB, 5, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 5>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
     else if (m == 6)
-        tile_block_any<real, ZB, 6, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 6>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
     else
-        tile_block_any<real, ZB, 7, false>(tab.inst, tx, ty, tz, 0, tab.dry != 0);
+        tile_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
 }
 
 // Plain tiles with two columns per thread (instances whose nx is a multiple
@@ -1125,7 +1324,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     long long gtotal = 0;
     for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
-    const dim3 block(LX, LY), half(LX, LY / 2);
+    const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS);
     for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
         LeanTable<real> t;
         t.inst = h_insts[q];
@@ -1144,9 +1343,9 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 #define SJ_ZB(Z)                                                                                             \
     case Z:                                                                                                  \
         t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
-        if (t.n_tiles) k_lean_multi<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_MULTI]>>>(t);          \
+        if (t.n_tiles) k_lean_multi<real, Z><<<(unsigned)t.n_tiles, halo, 0, sc[LEAN_MULTI]>>>(t);           \
         t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
-        if (t.n_tiles) k_lean_slab<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_SLAB]>>>(t);            \
+        if (t.n_tiles) k_lean_slab<real, Z><<<(unsigned)t.n_tiles, halo, 0, sc[LEAN_SLAB]>>>(t);             \
         t.tiles = T.list[LEAN_GENERAL], t.n_tiles = T.count[LEAN_GENERAL];                                   \
         if (gb) k_lean_general<real, Z><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st);                \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
