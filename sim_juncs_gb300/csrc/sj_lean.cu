@@ -87,7 +87,7 @@ constexpr int general_minb() { return sizeof(real) == 4 ? SJ_LEAN_GEN_MINB : 2; 
 // step reads into L2, one row per lane, so the loads of that plane find it
 // there.
 #ifndef SJ_LEAN_PF
-#define SJ_LEAN_PF 2
+#define SJ_LEAN_PF 1
 #endif
 constexpr int LEAN_PF = SJ_LEAN_PF;
 
@@ -297,16 +297,26 @@ __device__ __forceinline__ real source_sum(const InstDev<real>& I, int comp, int
 // subtracted from cv where the cell is in the slab (on).  psi_old is read
 // only for slab cells (non-coherently for the ping-pong H side, NC); AX
 // (compile time) removes axes a tile cannot touch.
-template <bool AX, bool ADD, bool NC, typename real>
-__device__ __forceinline__ void pml_term(real& cv, bool on, real b, real c, real d, const real* pin, real* pout,
-                                         unsigned x, bool store) {
+// the CPML term with the old psi value po already loaded
+template <bool AX, bool ADD, typename real>
+__device__ __forceinline__ void pml_term_v(real& cv, bool on, real b, real c, real d, real po, real* pout,
+                                           unsigned x, bool store) {
     if (!AX) return;
-    // branch-free: predicated load and store, the term folded in by select;
-    // outside the slab cv + (-0) and cv - (+0) leave cv, sign of zero included
-    const real po = on ? (NC ? __ldg(pin + x) : pin[x]) : real(0);
+    // branch-free: predicated store, the term folded in by select; outside
+    // the slab cv + (-0) and cv - (+0) leave cv, sign of zero included
     const real ps = fma(b, po, c * d);
     if (on && store) pout[x] = ps;
     cv = ADD ? cv + (on ? ps : real(-0.0)) : cv - (on ? ps : real(0));
+}
+// old psi of a cell in the slab (predicated load), 0 elsewhere
+template <bool AX, bool NC, typename real>
+__device__ __forceinline__ real psi_old(bool on, const real* pin, unsigned x) {
+    return (AX && on) ? (NC ? __ldg(pin + x) : pin[x]) : real(0);
+}
+template <bool AX, bool ADD, bool NC, typename real>
+__device__ __forceinline__ void pml_term(real& cv, bool on, real b, real c, real d, const real* pin, real* pout,
+                                         unsigned x, bool store) {
+    pml_term_v<AX, ADD>(cv, on, b, c, d, psi_old<AX, NC>(on, pin, x), pout, x, store);
 }
 
 // H^{n+1/2} = fma(-S, curl, H^{n-1/2}) [- dt J]
@@ -327,6 +337,11 @@ __device__ __forceinline__ real h_new(const InstDev<real>& I, int comp, real cv,
 template <int CA, typename real>
 __device__ __forceinline__ real e_new(const InstDev<real>& I, const real* cf, real e_old, real cv) {
     return fma(I.S * ldg(cf, CA), cv, e_old);
+}
+// the same with the combo's inverse eps_inf already loaded
+template <typename real>
+__device__ __forceinline__ real e_new_v(const InstDev<real>& I, real inv, real e_old, real cv) {
+    return fma(I.S * inv, cv, e_old);
 }
 
 // Slab axes a tile's footprint touches (bit a = axis a): the same footprint
@@ -675,6 +690,18 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
             hz = h_new<false>(I, 5, cv, ldg(hZ, o), false, i, j, k, 0);
         }
         if (store) {
+            // the E update's loads go ahead of the barrier (which the
+            // compiler does not move loads across): the combo's inverse
+            // eps_inf and the old E-side psi of the own cell
+            const bool eo = own && act;
+            real iv0 = 0, iv1 = 0, iv2 = 0;
+            if (eo) {
+                const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
+                iv0 = ldg(cf, 0), iv1 = ldg(cf, 1), iv2 = ldg(cf, 2);
+            }
+            const real qY0 = psi_old<SY, false>(eo && yo, peY, o), qY1 = psi_old<SY, false>(eo && yo, peY, o + vol);
+            const real qZ0 = psi_old<SZ, false>(eo && zo, peZ, o), qZ1 = psi_old<SZ, false>(eo && zo, peZ, o + vol);
+            const real qX0 = psi_old<SX, false>(eo && xo, peX, o), qX1 = psi_old<SX, false>(eo && xo, peX, o + vol);
             HaloPlane<real>& b = sh[k & 1];
             if ((own && w < LY - 1) || rowh) {
                 b.hx[rowh ? 0 : w + 1][lane] = hx;
@@ -695,28 +722,27 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
                     oHY[o] = hy;
                     oHZ[o] = hz;
                     // E^{n+1} at the own cell
-                    const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
                     const bool si = !dry;
                     {
                         const real d1 = hz - hz_ym, d2 = hy - hyp;
                         real cv = d1 - d2;
-                        pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
-                        pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
-                        oEX[o] = e_new<0>(I, cf, ex_c, cv);
+                        pml_term_v<SY, true>(cv, yo, byi, cyi, d1, qY0, peY, o, si);
+                        pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, qZ0, peZ, o, si);
+                        oEX[o] = e_new_v(I, iv0, ex_c, cv);
                     }
                     {
                         const real d1 = hx - hxp, d2 = hz - hz_xm;
                         real cv = d1 - d2;
-                        pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
-                        pml_term<SX, false, false>(cv, xo, bxi, cxi, d2, peX, peX, o, si);
-                        oEY[o] = e_new<1>(I, cf, ey_c, cv);
+                        pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, qZ1, peZ + vol, o, si);
+                        pml_term_v<SX, false>(cv, xo, bxi, cxi, d2, qX0, peX, o, si);
+                        oEY[o] = e_new_v(I, iv1, ey_c, cv);
                     }
                     {
                         const real d1 = hy - hy_xm, d2 = hx - hx_ym;
                         real cv = d1 - d2;
-                        pml_term<SX, true, false>(cv, xo, bxi, cxi, d1, peX + vol, peX + vol, o, si);
-                        pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
-                        oEZ[o] = e_new<2>(I, cf, ez, cv);
+                        pml_term_v<SX, true>(cv, xo, bxi, cxi, d1, qX1, peX + vol, o, si);
+                        pml_term_v<SY, false>(cv, yo, byi, cyi, d2, qY1, peY + vol, o, si);
+                        oEZ[o] = e_new_v(I, iv2, ez, cv);
                     }
                 }
             }
