@@ -583,6 +583,36 @@ struct HaloPlane {
     real xz[LY];
 };
 
+// The H update's inputs of one plane at a warp's cell: E of the plane and
+// of the one above, the x+1 / y+1 neighbours, old H and the old H-side psi
+// (Hx: y, z; Hy: z, x; Hz: x, y; 0 outside the slabs), loaded together so
+// that they are all in flight at once.  ok = false loads nothing (zeros).
+template <typename real>
+struct HaloIn {
+    real ex_n, ey_n, ez, ez_xp, ez_yp, ey_xp, ex_yp, hx, hy, hz;
+    real qy0, qz0, qz1, qx0, qx1, qy1;
+};
+template <typename real, bool SX, bool SY, bool SZ, bool EDGE>
+__device__ __forceinline__ HaloIn<real> halo_in(const InstDev<real>& I, unsigned o, int k, bool ok, bool xp,
+                                                bool yp, bool xo, bool yo) {
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
+    const bool kp = ok && (!EDGE || k + 1 < I.nz);
+    const bool zo = SZ && (k < I.pl[2] || k >= I.nz - I.ph[2]);
+    HaloIn<real> r;
+    r.ex_n = ldz(I.F[0][0], o + plane, kp), r.ey_n = ldz(I.F[0][1], o + plane, kp);
+    r.ez = ldz(I.F[0][2], o, ok);
+    r.ez_xp = ldz(I.F[0][2], o + 1, ok && xp), r.ez_yp = ldz(I.F[0][2], o + px, ok && yp);
+    r.ey_xp = ldz(I.F[0][1], o + 1, ok && xp), r.ex_yp = ldz(I.F[0][0], o + px, ok && yp);
+    r.hx = ldz(I.F[0][3], o, ok), r.hy = ldz(I.F[0][4], o, ok), r.hz = ldz(I.F[0][5], o, ok);
+    r.qy0 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, o);
+    r.qy1 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, o + vol);
+    r.qz0 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, o);
+    r.qz1 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, o + vol);
+    r.qx0 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, o);
+    r.qx1 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, o + vol);
+    return r;
+}
+
 template <typename real, int ZB, int MASK, bool EDGE>
 __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
                                           HaloPlane<real>* sh) {
@@ -601,19 +631,12 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
     const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
     const real* eX = I.F[0][0];
     const real* eY = I.F[0][1];
-    const real* eZ = I.F[0][2];
-    const real* hX = I.F[0][3];
-    const real* hY = I.F[0][4];
-    const real* hZ = I.F[0][5];
     real* oEX = I.F[1][0];
     real* oEY = I.F[1][1];
     real* oEZ = I.F[1][2];
     real* oHX = I.F[1][3];
     real* oHY = I.F[1][4];
     real* oHZ = I.F[1][5];
-    const real* hiX = SX ? I.psiH[0][0] : nullptr;
-    const real* hiY = SY ? I.psiH[0][1] : nullptr;
-    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
     real* hoX = SX ? I.psiH[1][0] : nullptr;
     real* hoY = SY ? I.psiH[1][1] : nullptr;
     real* hoZ = SZ ? I.psiH[1][2] : nullptr;
@@ -647,7 +670,6 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
     volatile unsigned long long* lr =
         lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, lane, xt, yo));
     for (; k < z1; ++k, o += plane) {
-        const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;  // block-uniform
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
         if (LEAN_PF > 0) {
@@ -660,34 +682,33 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
             const real* pr = I.prof[2];
             bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
         }
-        const real ex_n = ldz(eX, o + plane, kp), ey_n = ldz(eY, o + plane, kp);
-        const real ez = ldg(eZ, o);
-        const real ez_xp = ldz(eZ, o + 1, xp), ez_yp = ldz(eZ, o + px, yp);
-        const real ey_xp = ldz(eY, o + 1, xp), ex_yp = ldz(eX, o + px, yp);
+        // every load of the H update issued together
+        const HaloIn<real> c = halo_in<real, SX, SY, SZ, EDGE>(I, o, k, true, xp, yp, xo, yo);
+        const real ex_n = c.ex_n, ey_n = c.ey_n, ez = c.ez;
         const bool sp = store && !dry && own && act;
 
         // H^{n+1/2} at the warp's cells
         real hx, hy, hz;
         {
-            const real d1 = ez_yp - ez, d2 = ey_n - ey_c;
+            const real d1 = c.ez_yp - ez, d2 = ey_n - ey_c;
             real cv = d1 - d2;
-            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o, sp);
-            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o, sp);
-            hx = h_new<false>(I, 3, cv, ldg(hX, o), false, i, j, k, 0);
+            pml_term_v<SY, true>(cv, yo, byh, cyh, d1, c.qy0, hoY, o, sp);
+            pml_term_v<SZ, false>(cv, zo, bzh, czh, d2, c.qz0, hoZ, o, sp);
+            hx = h_new<false>(I, 3, cv, c.hx, false, i, j, k, 0);
         }
         {
-            const real d1 = ex_n - ex_c, d2 = ez_xp - ez;
+            const real d1 = ex_n - ex_c, d2 = c.ez_xp - ez;
             real cv = d1 - d2;
-            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o, sp);
-            pml_term<SX, false, true>(cv, xo, bxh, cxh, d2, hiX, hoX, o, sp);
-            hy = h_new<false>(I, 4, cv, ldg(hY, o), false, i, j, k, 0);
+            pml_term_v<SZ, true>(cv, zo, bzh, czh, d1, c.qz1, hoZ + vol, o, sp);
+            pml_term_v<SX, false>(cv, xo, bxh, cxh, d2, c.qx0, hoX, o, sp);
+            hy = h_new<false>(I, 4, cv, c.hy, false, i, j, k, 0);
         }
         {
-            const real d1 = ey_xp - ey_c, d2 = ex_yp - ex_c;
+            const real d1 = c.ey_xp - ey_c, d2 = c.ex_yp - ex_c;
             real cv = d1 - d2;
-            pml_term<SX, true, true>(cv, xo, bxh, cxh, d1, hiX + vol, hoX + vol, o, sp);
-            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o, sp);
-            hz = h_new<false>(I, 5, cv, ldg(hZ, o), false, i, j, k, 0);
+            pml_term_v<SX, true>(cv, xo, bxh, cxh, d1, c.qx1, hoX + vol, o, sp);
+            pml_term_v<SY, false>(cv, yo, byh, cyh, d2, c.qy1, hoY + vol, o, sp);
+            hz = h_new<false>(I, 5, cv, c.hz, false, i, j, k, 0);
         }
         if (store) {
             // the E update's loads go ahead of the barrier (which the
