@@ -110,6 +110,8 @@ struct HostInst {
     double* d_mon = nullptr;
     long long mon_cap = 0;
     std::vector<uint32_t> keys;      // combo -> (cx | cy<<8 | cz<<16)
+    std::vector<real> coef;          // combo coefficient table (host copy of I.coef)
+    std::vector<real> prof[3];       // CPML profiles (host copies of I.prof)
     std::vector<double> des_eps;     // design region eps per voxel (empty: none)
     real* d_dinv = nullptr;          // its inverse on the device
     long long voxels = 0;
@@ -153,6 +155,8 @@ struct sj_sim {
     int lean_zb = -1;                  // z-segment length the tile lists were built for
     void* d_tiles = nullptr;           // tile lists of all instances and classes
     std::vector<LeanTiles> ltiles;     // per instance
+    std::vector<LeanGroup> lgroups;    // instances sharing tile launches (every instance in one)
+    std::vector<std::vector<int>> lmembers;  // per group: its instances, member order
     void* d_fix = nullptr;             // correction block tables (E sources, polarisations)
     LeanFix lfix{};
     cudaStream_t side[LEAN_STREAMS] = {};
@@ -417,6 +421,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
     }
     I.coef = sim->upload(coef);
     I.cflag = sim->upload(cflag);
+    H.coef = coef;
 
     // ---- dispersive bounding box and polarisation storage
     {
@@ -496,6 +501,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
             if (on[i]) fail(SJ_E_INVALID, "PML profile is not confined to the faces");
         I.pl[a] = pl, I.ph[a] = ph;
         I.prof[a] = sim->upload(prof);
+        H.prof[a] = prof;
         const long long w = pl + ph;
         if (w > 0) {  // full-grid layout; only the slab voxels are ever touched
             I.psiE[a] = (real*)sim->dalloc(2 * vol * sizeof(real));
@@ -793,6 +799,16 @@ void prepare_lean(sj_sim* sim) {
             all.insert(all.end(), lists[c].begin(), lists[c].end());
         }
     }
+    // a group's launches use the lead's lists: its members' must be equal
+    for (const auto& mem : sim->lmembers)
+        for (size_t r = 1; r < mem.size(); ++r)
+            for (int c = 0; c < LEAN_CLASSES; ++c) {
+                const long long n = sim->ltiles[mem[0]].count[c];
+                const unsigned* a = all.data() + off[(size_t)mem[0] * LEAN_CLASSES + c];
+                const unsigned* b = all.data() + off[(size_t)mem[r] * LEAN_CLASSES + c];
+                if (sim->ltiles[mem[r]].count[c] != n || (n && memcmp(a, b, n * sizeof(unsigned)) != 0))
+                    fail(SJ_E_INVALID, "internal: members of a launch group have different tile lists");
+            }
     sim->dfree(sim->d_tiles);
     sim->d_tiles = sim->upload(all);
     const unsigned* base = reinterpret_cast<const unsigned*>(sim->d_tiles);
@@ -847,8 +863,8 @@ cudaError_t launch_one(sj_sim* sim) {
     cudaError_t e;
     if (sim->schedule == SJ_SCHED_FUSED) {
         prepare_lean<real>(sim);
-        e = launch_lean_step<real>(dv.data(), d, sim->ltiles.data(), sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur,
-                                   sim->d_state, lean_streams(sim));
+        e = launch_lean_step<real>(dv.data(), d, sim->ltiles.data(), sim->lgroups.data(), (int)sim->lgroups.size(),
+                                   sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur, sim->d_state, lean_streams(sim));
     } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
@@ -878,11 +894,13 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
         prepare_lean<real>(sim);
         const LeanTiles* lt = sim->ltiles.data();
         const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
-        ck(launch_lean_step<real>(dv.data(), d, lt, sim->lfix, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+        ck(launch_lean_step<real>(dv.data(), d, lt, sim->lgroups.data(), (int)sim->lgroups.size(), sim->lfix,
+                                  sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
            "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
-            ck(launch_lean_step<real>(dv.data(), d, lt, sim->lfix, sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+            ck(launch_lean_step<real>(dv.data(), d, lt, sim->lgroups.data(), (int)sim->lgroups.size(), sim->lfix,
+                                      sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
                "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
@@ -1313,6 +1331,93 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
     for (void* p : temps) sim->dfree(p);
 }
 
+template <typename T>
+bool same_bits(const std::vector<T>& a, const std::vector<T>& b) {
+    return a.size() == b.size() && (a.empty() || memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+
+// Can instances a and b share tile launches?  Their tile lists depend on
+// the grid, the CPML slabs and the H-source boxes; the tile kernels read the
+// time step, the CPML profiles and the coefficient table from the lead's
+// descriptor, so those must agree bit for bit.
+template <typename real>
+bool same_tiles(const HostInst<real>& ha, const InstDev<real>& a, const HostInst<real>& hb, const InstDev<real>& b) {
+    if (a.nx != b.nx || a.ny != b.ny || a.nz != b.nz || a.px != b.px) return false;
+    if (memcmp(&a.S, &b.S, sizeof(real)) != 0) return false;
+    for (int ax = 0; ax < 3; ++ax)
+        if (a.pl[ax] != b.pl[ax] || a.ph[ax] != b.ph[ax] || !same_bits(ha.prof[ax], hb.prof[ax])) return false;
+    if (a.ncoef != b.ncoef || a.n_combos != b.n_combos || !same_bits(ha.coef, hb.coef)) return false;
+    auto hboxes = [](const InstDev<real>& I) {
+        std::vector<int> v;
+        for (int s = 0; s < I.n_src; ++s)
+            if (I.src[s].comp >= 3) {
+                v.push_back(I.src[s].comp);
+                for (int ax = 0; ax < 3; ++ax) v.push_back(I.src[s].lo[ax]), v.push_back(I.src[s].n[ax]);
+            }
+        return v;
+    };
+    return hboxes(a) == hboxes(b);
+}
+
+// Move the arrays of `members` (one group, lead first) into one allocation
+// per array: fields and combo bytes of member r at r * vol elements from the
+// lead's, psi at r * 2 * vol.
+template <typename real>
+void pack_group(sj_sim* sim, const std::vector<int>& members) {
+    auto& dv = devv<real>(sim);
+    const long long vol = dv[members[0]].vol;
+    const size_t G = members.size();
+    cudaStream_t st = sim->stream;
+    auto pack = [&](auto get, size_t bytes) {  // get(q) -> reference to instance q's pointer
+        char* arena = (char*)sim->dalloc(G * bytes, false);
+        for (size_t r = 0; r < G; ++r)
+            ck(cudaMemcpyAsync(arena + r * bytes, get(members[r]), bytes, cudaMemcpyDeviceToDevice, st), "pack");
+        ck(cudaStreamSynchronize(st), "pack sync");
+        for (size_t r = 0; r < G; ++r) {
+            auto& ptr = get(members[r]);
+            sim->dfree((void*)ptr);
+            ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(arena + r * bytes);
+        }
+    };
+    for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 6; ++c) pack([&](int q) -> real*& { return dv[q].F[b][c]; }, vol * sizeof(real));
+    pack([&](int q) -> const uint8_t*& { return dv[q].combo; }, (size_t)vol);
+    for (int a = 0; a < 3; ++a) {
+        if (!dv[members[0]].psiE[a]) continue;
+        pack([&](int q) -> real*& { return dv[q].psiE[a]; }, 2 * vol * sizeof(real));
+        for (int b = 0; b < 2; ++b) pack([&](int q) -> real*& { return dv[q].psiH[b][a]; }, 2 * vol * sizeof(real));
+    }
+}
+
+// Sort the instances into LeanGroups (first fit, in instance order) and
+// pack each group of two or more.  A group's psi offsets (2 r vol + 2 vol)
+// stay below 2^32 elements.
+template <typename real>
+void group_instances(sj_sim* sim) {
+    auto& hv = hostv<real>(sim);
+    auto& dv = devv<real>(sim);
+    std::vector<std::vector<int>> groups;
+    for (int q = 0; q < sim->n_inst; ++q) {
+        bool placed = false;
+        for (auto& g : groups) {
+            const int lead = g[0];
+            const long long cap = ((1LL << 32) - 1) / (2 * dv[lead].vol);
+            if ((long long)g.size() < std::min(cap, 65535LL) && same_tiles(hv[lead], dv[lead], hv[q], dv[q])) {
+                g.push_back(q);
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) groups.push_back({q});
+    }
+    sim->lgroups.clear();
+    sim->lmembers = groups;
+    for (const auto& g : groups) {
+        if (g.size() > 1) pack_group<real>(sim, g);
+        sim->lgroups.push_back(LeanGroup{g[0], (int)g.size()});
+    }
+}
+
 template <typename real>
 void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
     auto& hv = hostv<real>(sim);
@@ -1320,6 +1425,7 @@ void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
     hv.resize(n);
     dv.resize(n);
     for (int q = 0; q < n; ++q) build_instance<real>(sim, insts[q], hv[q], dv[q]);
+    group_instances<real>(sim);
     upload_table<real>(sim);
 }
 
@@ -1569,8 +1675,10 @@ int32_t sj_launches_per_step(const sj_sim* sim) {
         else
             lean_fix_blocks(sim->h32.data(), sim->n_inst, passes);
         for (int p = 0; p < LEAN_FIX_PASSES; ++p) fx.count[p] = (long long)passes[p].size();
-        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), fx, sim->n_inst)
-                                        : lean_launches(sim->h32.data(), lt.data(), fx, sim->n_inst);
+        const LeanGroup* lg = sim->lgroups.data();
+        const int ng = (int)sim->lgroups.size();
+        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), lg, ng, fx, sim->n_inst)
+                                        : lean_launches(sim->h32.data(), lt.data(), lg, ng, fx, sim->n_inst);
     }
     if (sim->schedule == SJ_SCHED_TMA) return 1;
     int maxp = 0;

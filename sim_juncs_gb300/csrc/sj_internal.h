@@ -118,9 +118,10 @@ cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState
 // Fused (lean) schedule.  Tiles (32 x 8 columns x zb planes) fall into four
 // classes by what their footprint touches: CPML slabs of no axis (plain),
 // of one axis (slab) or of several (multi), or an H source (general).  E
-// sources and polarisations are corrections applied after the tiles.  Each
-// step is one launch per instance and non-empty class; the launch carries
-// the instance descriptor as a kernel parameter.
+// sources and polarisations are corrections applied after the tiles.  The
+// plain, slab and multi tiles of a group of instances (LeanGroup) run as one
+// launch per class, blockIdx.y = member; general tiles as one launch per
+// instance.  A launch carries its descriptor as a kernel parameter.
 enum { LEAN_PLAIN = 0, LEAN_SLAB = 1, LEAN_MULTI = 2, LEAN_GENERAL = 3, LEAN_CLASSES = 4 };
 template <typename real>
 struct LeanTable {
@@ -129,6 +130,16 @@ struct LeanTable {
     long long n_tiles;          // tiles of this launch (general: probe blocks follow)
     int dry;                    // 1 = time only: no step advance, no in-place stores
     unsigned step_blocks;       // general-launch blocks of the whole step
+    unsigned qvol;              // group member r's fields at + r * qvol elements, psi at + 2 r * qvol
+};
+// Instances whose tile kernels share launches: equal grid, time step, CPML
+// profiles, coefficient table and H-source boxes (hence equal tile lists),
+// with every field, combo and psi array of member r at a fixed offset from
+// the lead's: r * vol elements (fields, combo), r * 2 * vol (psi).  Member
+// 0 is the lead; the host keeps which instance is member r.
+struct LeanGroup {
+    int lead;
+    int n;
 };
 // Device tile lists of one instance, by class.
 struct LeanTiles {
@@ -148,11 +159,13 @@ struct LeanFix {
 template <typename real>
 void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes);
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanFix& fix, int n_inst);
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanGroup* groups, int n_groups,
+                  const LeanFix& fix, int n_inst);
 // Streams of one fused step: LEAN_SETS sets of one stream per tile class,
-// forked from `main` and joined back into it with the events; instance q's
-// launches go to set q % LEAN_SETS, so the small launches of many instances
-// overlap (side streams null: all on `main`).
+// forked from `main` and joined back into it with the events; group g's
+// launches go to set g % LEAN_SETS (instance q's general launch to set
+// q % LEAN_SETS), so the launches of many groups overlap (side streams
+// null: all on `main`).
 constexpr int LEAN_SETS = 4;
 constexpr int LEAN_STREAMS = LEAN_SETS * LEAN_CLASSES;
 struct LeanStreams {
@@ -162,8 +175,8 @@ struct LeanStreams {
 };
 template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
-                             const LeanFix& fix, int n_inst, int zb, int dry, int cur, DevState* st,
-                             const LeanStreams& ls);
+                             const LeanGroup* groups, int n_groups, const LeanFix& fix, int n_inst, int zb, int dry,
+                             int cur, DevState* st, const LeanStreams& ls);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>

@@ -4,34 +4,37 @@
 // H^{n+1/2}, E^{n+1} (buffer cur^1): each field component crosses HBM once in
 // and once out per step.
 //
-// A thread owns one (i, j) column and marches along z over a segment of ZB
-// planes; a block is a 32 x 8 tile of columns.  For each plane k the thread
-// updates H at its own cell and recomputes H at (i-1, j) and (i, j-1) — the
-// two neighbours the E update needs, owned by other threads — instead of
-// exchanging them, so the kernels need no shared memory and no barrier; the
-// neighbour values come from L1/L2.  E and H of plane k+1 that become plane
-// k's values next iteration are carried in registers, as is the own H of
-// plane k-1.  A segment starting at z0 > 0 first recomputes H of plane z0-1
-// (owned by the previous segment).  The ping-pong buffers (fields and H-side
-// CPML psi) make the recomputation race-free: nothing a block reads is
-// written during the step.
+// A block takes a tile of 32 x 8 (i, j) columns and marches along z over a
+// segment of ZB planes; a segment starting at z0 > 0 first updates H of
+// plane z0-1 (owned by the previous segment) without storing it.  The E
+// update at (i, j, k) needs H of the cells at x-1 and y-1, which other
+// threads (or other tiles) own; how a kernel gets them depends on the tile
+// class.  The ping-pong buffers (fields and H-side CPML psi) keep every
+// variant race-free: nothing a block reads is written during the step.
 //
-// Four kernels share the tiles of a step, by what a tile's footprint (own
-// cells and the recomputed x-1/y-1/z-1 neighbours) touches; the host sorts
-// the tiles into one list per class.  k_lean_plain takes tiles clear of CPML
-// slabs, sources and dispersive voxels: a short loop that keeps few
-// registers and runs at high occupancy.  k_lean_slab takes tiles in the
-// slabs of exactly one axis (most of the CPML volume) and k_lean_multi those
-// in the slabs of two or three (edges, corners), both compiled per axis set
-// so the other axes' terms vanish.  k_lean_general takes tiles with a source
-// or dispersive voxel and the probe blocks; its blocks (the only ones that
-// read the step counter) count themselves, and the last one advances the
-// step.  A step launches each non-empty class of each instance on streams
-// forked from the caller's (one per class and instance set), so the kernels
+// The host sorts the tiles into one list per class, by what a tile's
+// footprint (own cells and the x-1/y-1/z-1 neighbours) touches:
+//   plain   (k_lean_plain2 / k_lean_plain): no CPML slab and no H source.
+//           Two columns per thread where rows are whole (nx % 32 == 0): x-1
+//           H from the neighbouring lane by shuffle, y-1 H recomputed from
+//           L1/L2; otherwise one column per thread recomputing both.
+//   slab    (k_lean_slab): the CPML slabs of one axis; multi (k_lean_multi):
+//           of two or three.  Ten warps per tile: the 8 rows plus one warp
+//           for the row below the tile and one for the column left of it,
+//           which update H only; x-1 H comes by shuffle, y-1 H through a
+//           double-buffered shared plane (one barrier per plane).  Compiled
+//           per axis set, so the other axes' terms vanish.
+//   general (k_lean_general): an H source in the footprint; also runs the
+//           probe blocks, and its blocks (the only ones that read the step
+//           counter) count themselves: the last advances the step.
+// Instances with the same grid, CPML and coefficient table form a group
+// (LeanGroup) whose arrays sit at fixed strides: one launch per class covers
+// the group's tiles (blockIdx.y = member).  The launches of a step go to
+// streams forked from the caller's, one per class and group set, so they
 // overlap; after they join, small correction kernels add the E sources and
-// the polarisation ADE on their cells only.  All evaluate one update formula,
-// so a voxel's result does not depend on which kernel (or which tiling)
-// updated it:
+// the polarisation ADE on their cells only.  All evaluate one update
+// formula, so a voxel's result does not depend on which kernel (or which
+// tiling) updated it:
 //   H^{n+1/2} = fma(-S, curl E, H^{n-1/2}) [- dt J_H]
 //   E^{n+1}   = fma(S ε∞⁻¹, curl H, E^n)
 //               [then fma(-ε∞⁻¹, dt J_s, ·) per E source s, in order]
@@ -148,16 +151,19 @@ __host__ __device__ inline bool tile_edge(const InstDev<real>& I, int tx, int ty
 // row is one word: the array's address (16-byte aligned) with bit 0 set for
 // a z psi row and bit 1 for a byte array; 0 = no row.  The word waits in a
 // shared-memory slot of the thread and is reloaded on every plane, so it
-// holds no register across the march.
+// holds no register across the march.  The element offset a row is
+// prefetched at is a field offset; psi rows add qf (a group member's psi
+// sits twice as far from the lead's as its fields).
 template <typename real, bool SX, bool SY, bool SZ>
-__device__ __forceinline__ unsigned long long lane_row(const InstDev<real>& I, int l, bool xt, bool yt) {
+__device__ __forceinline__ unsigned long long lane_row(const InstDev<real>& I, int l, bool xt, bool yt,
+                                                       unsigned qf = 0) {
     if (l < 6) return (unsigned long long)I.F[0][l];
     if (l == 6) return (unsigned long long)I.combo | 2ull;
     if (l < 19) {
         const int a = (l - 7) >> 2, q = (l - 7) & 3;
         if (a == 0 ? SX && xt : (a == 1 ? SY && yt : SZ)) {
             const real* b = q < 2 ? I.psiH[0][a] : I.psiE[a];
-            return (unsigned long long)(b + ((q & 1) ? I.vol : 0)) | (a == 2 ? 1ull : 0ull);
+            return (unsigned long long)(b + qf + ((q & 1) ? I.vol : 0)) | (a == 2 ? 1ull : 0ull);
         }
     }
     return 0;
@@ -183,7 +189,7 @@ __device__ __forceinline__ void prefetch_lane_row(volatile unsigned long long* s
 // EDGE = false: the tile's footprint and its z+1 plane stay inside the grid,
 // so no load needs a bounds predicate.
 template <typename real, int ZB, bool EDGE>
-__device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int ty, int tz) {
+__device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int ty, int tz, unsigned qf) {
     const int i = tx * LX + threadIdx.x, j = ty * LY + threadIdx.y;
     const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
     if (EDGE && (i >= I.nx || j >= I.ny)) return;
@@ -204,7 +210,7 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
     const bool xm = !EDGE || i > 0, ym = !EDGE || j > 0, xp = !EDGE || i + 1 < I.nx, yp = !EDGE || j + 1 < I.ny;
 
     int k = z0 > 0 ? z0 - 1 : 0;
-    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i + qf;  // group member blockIdx.y
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real exm_c = ldz(eX, o - 1, xm), eym_c = ldz(eY, o - px, ym);
     real hxp = 0, hyp = 0;
@@ -586,15 +592,16 @@ struct HaloPlane {
 // The H update's inputs of one plane at a warp's cell: E of the plane and
 // of the one above, the x+1 / y+1 neighbours, old H and the old H-side psi
 // (Hx: y, z; Hy: z, x; Hz: x, y; 0 outside the slabs), loaded together so
-// that they are all in flight at once.  ok = false loads nothing (zeros).
+// that they are all in flight at once.  o: the cell's field offset, op: its
+// psi offset; ok = false loads nothing (zeros).
 template <typename real>
 struct HaloIn {
     real ex_n, ey_n, ez, ez_xp, ez_yp, ey_xp, ex_yp, hx, hy, hz;
     real qy0, qz0, qz1, qx0, qx1, qy1;
 };
 template <typename real, bool SX, bool SY, bool SZ, bool EDGE>
-__device__ __forceinline__ HaloIn<real> halo_in(const InstDev<real>& I, unsigned o, int k, bool ok, bool xp,
-                                                bool yp, bool xo, bool yo) {
+__device__ __forceinline__ HaloIn<real> halo_in(const InstDev<real>& I, unsigned o, unsigned op, int k, bool ok,
+                                                bool xp, bool yp, bool xo, bool yo) {
     const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
     const bool kp = ok && (!EDGE || k + 1 < I.nz);
     const bool zo = SZ && (k < I.pl[2] || k >= I.nz - I.ph[2]);
@@ -604,18 +611,18 @@ __device__ __forceinline__ HaloIn<real> halo_in(const InstDev<real>& I, unsigned
     r.ez_xp = ldz(I.F[0][2], o + 1, ok && xp), r.ez_yp = ldz(I.F[0][2], o + px, ok && yp);
     r.ey_xp = ldz(I.F[0][1], o + 1, ok && xp), r.ex_yp = ldz(I.F[0][0], o + px, ok && yp);
     r.hx = ldz(I.F[0][3], o, ok), r.hy = ldz(I.F[0][4], o, ok), r.hz = ldz(I.F[0][5], o, ok);
-    r.qy0 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, o);
-    r.qy1 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, o + vol);
-    r.qz0 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, o);
-    r.qz1 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, o + vol);
-    r.qx0 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, o);
-    r.qx1 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, o + vol);
+    r.qy0 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, op);
+    r.qy1 = psi_old<SY, true>(ok && yo, SY ? I.psiH[0][1] : nullptr, op + vol);
+    r.qz0 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, op);
+    r.qz1 = psi_old<SZ, true>(ok && zo, SZ ? I.psiH[0][2] : nullptr, op + vol);
+    r.qx0 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, op);
+    r.qx1 = psi_old<SX, true>(ok && xo, SX ? I.psiH[0][0] : nullptr, op + vol);
     return r;
 }
 
 template <typename real, int ZB, int MASK, bool EDGE>
 __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
-                                          HaloPlane<real>* sh) {
+                                          HaloPlane<real>* sh, unsigned qf) {
     constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
     const int w = threadIdx.y, lane = threadIdx.x;
     const bool own = w < LY, rowh = w == LY, colh = w == LY + 1;
@@ -660,15 +667,16 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
 
     int k = z0 > 0 ? z0 - 1 : 0;
     const int k0 = k;
-    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+    // field offsets (and psi offsets, + qf) of group member blockIdx.y
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i + qf;
     real ex_c = ldg(eX, o), ey_c = ldg(eY, o);
     real hxp = 0, hyp = 0;  // H^{n+1/2} of plane k-1 at the own cell
     // row prefetch: the tile rows and the row below them (the column warp's
     // cells are not a row)
     const bool xt = SX && (imax(i0 - 1, 0) < I.pl[0] || imin(i0 + LX, nx) - 1 >= nx - I.ph[0]);
-    const unsigned orow = (unsigned)k * plane + (unsigned)j * px + (unsigned)i0;
+    const unsigned orow = (unsigned)k * plane + (unsigned)j * px + (unsigned)i0 + qf;
     volatile unsigned long long* lr =
-        lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, lane, xt, yo));
+        lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, lane, xt, yo, qf));
     for (; k < z1; ++k, o += plane) {
         const bool store = k >= z0;  // block-uniform
         const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
@@ -683,7 +691,8 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
             bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
         }
         // every load of the H update issued together
-        const HaloIn<real> c = halo_in<real, SX, SY, SZ, EDGE>(I, o, k, true, xp, yp, xo, yo);
+        const unsigned op = o + qf;
+        const HaloIn<real> c = halo_in<real, SX, SY, SZ, EDGE>(I, o, op, k, true, xp, yp, xo, yo);
         const real ex_n = c.ex_n, ey_n = c.ey_n, ez = c.ez;
         const bool sp = store && !dry && own && act;
 
@@ -692,22 +701,22 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
         {
             const real d1 = c.ez_yp - ez, d2 = ey_n - ey_c;
             real cv = d1 - d2;
-            pml_term_v<SY, true>(cv, yo, byh, cyh, d1, c.qy0, hoY, o, sp);
-            pml_term_v<SZ, false>(cv, zo, bzh, czh, d2, c.qz0, hoZ, o, sp);
+            pml_term_v<SY, true>(cv, yo, byh, cyh, d1, c.qy0, hoY, op, sp);
+            pml_term_v<SZ, false>(cv, zo, bzh, czh, d2, c.qz0, hoZ, op, sp);
             hx = h_new<false>(I, 3, cv, c.hx, false, i, j, k, 0);
         }
         {
             const real d1 = ex_n - ex_c, d2 = c.ez_xp - ez;
             real cv = d1 - d2;
-            pml_term_v<SZ, true>(cv, zo, bzh, czh, d1, c.qz1, hoZ + vol, o, sp);
-            pml_term_v<SX, false>(cv, xo, bxh, cxh, d2, c.qx0, hoX, o, sp);
+            pml_term_v<SZ, true>(cv, zo, bzh, czh, d1, c.qz1, hoZ + vol, op, sp);
+            pml_term_v<SX, false>(cv, xo, bxh, cxh, d2, c.qx0, hoX, op, sp);
             hy = h_new<false>(I, 4, cv, c.hy, false, i, j, k, 0);
         }
         {
             const real d1 = c.ey_xp - ey_c, d2 = c.ex_yp - ex_c;
             real cv = d1 - d2;
-            pml_term_v<SX, true>(cv, xo, bxh, cxh, d1, c.qx1, hoX + vol, o, sp);
-            pml_term_v<SY, false>(cv, yo, byh, cyh, d2, c.qy1, hoY + vol, o, sp);
+            pml_term_v<SX, true>(cv, xo, bxh, cxh, d1, c.qx1, hoX + vol, op, sp);
+            pml_term_v<SY, false>(cv, yo, byh, cyh, d2, c.qy1, hoY + vol, op, sp);
             hz = h_new<false>(I, 5, cv, c.hz, false, i, j, k, 0);
         }
         if (store) {
@@ -720,9 +729,9 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
                 const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
                 iv0 = ldg(cf, 0), iv1 = ldg(cf, 1), iv2 = ldg(cf, 2);
             }
-            const real qY0 = psi_old<SY, false>(eo && yo, peY, o), qY1 = psi_old<SY, false>(eo && yo, peY, o + vol);
-            const real qZ0 = psi_old<SZ, false>(eo && zo, peZ, o), qZ1 = psi_old<SZ, false>(eo && zo, peZ, o + vol);
-            const real qX0 = psi_old<SX, false>(eo && xo, peX, o), qX1 = psi_old<SX, false>(eo && xo, peX, o + vol);
+            const real qY0 = psi_old<SY, false>(eo && yo, peY, op), qY1 = psi_old<SY, false>(eo && yo, peY, op + vol);
+            const real qZ0 = psi_old<SZ, false>(eo && zo, peZ, op), qZ1 = psi_old<SZ, false>(eo && zo, peZ, op + vol);
+            const real qX0 = psi_old<SX, false>(eo && xo, peX, op), qX1 = psi_old<SX, false>(eo && xo, peX, op + vol);
             HaloPlane<real>& b = sh[k & 1];
             if ((own && w < LY - 1) || rowh) {
                 b.hx[rowh ? 0 : w + 1][lane] = hx;
@@ -747,22 +756,22 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
                     {
                         const real d1 = hz - hz_ym, d2 = hy - hyp;
                         real cv = d1 - d2;
-                        pml_term_v<SY, true>(cv, yo, byi, cyi, d1, qY0, peY, o, si);
-                        pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, qZ0, peZ, o, si);
+                        pml_term_v<SY, true>(cv, yo, byi, cyi, d1, qY0, peY, op, si);
+                        pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, qZ0, peZ, op, si);
                         oEX[o] = e_new_v(I, iv0, ex_c, cv);
                     }
                     {
                         const real d1 = hx - hxp, d2 = hz - hz_xm;
                         real cv = d1 - d2;
-                        pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, qZ1, peZ + vol, o, si);
-                        pml_term_v<SX, false>(cv, xo, bxi, cxi, d2, qX0, peX, o, si);
+                        pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, qZ1, peZ + vol, op, si);
+                        pml_term_v<SX, false>(cv, xo, bxi, cxi, d2, qX0, peX, op, si);
                         oEY[o] = e_new_v(I, iv1, ey_c, cv);
                     }
                     {
                         const real d1 = hy - hy_xm, d2 = hx - hx_ym;
                         real cv = d1 - d2;
-                        pml_term_v<SX, true>(cv, xo, bxi, cxi, d1, qX1, peX + vol, o, si);
-                        pml_term_v<SY, false>(cv, yo, byi, cyi, d2, qY1, peY + vol, o, si);
+                        pml_term_v<SX, true>(cv, xo, bxi, cxi, d1, qX1, peX + vol, op, si);
+                        pml_term_v<SY, false>(cv, yo, byi, cyi, d2, qY1, peY + vol, op, si);
                         oEZ[o] = e_new_v(I, iv2, ez, cv);
                     }
                 }
@@ -795,7 +804,7 @@ __device__ __forceinline__ typename Pair<real>::T ld2z(const real* p, unsigned o
 // Rows beyond ny (EDGE only) run with a clamped row and store nothing, so
 // that every lane reaches the shuffles.
 template <typename real, int ZB, int MASK, bool EDGE>
-__device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty, int tz, bool dry) {
+__device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty, int tz, bool dry, unsigned qf) {
     using V2 = typename Pair<real>::T;
     constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
     const int lane = threadIdx.x & 15, half = threadIdx.x >> 4;
@@ -818,15 +827,17 @@ __device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty
     real* oHX = I.F[1][3];
     real* oHY = I.F[1][4];
     real* oHZ = I.F[1][5];
-    const real* hiX = SX ? I.psiH[0][0] : nullptr;
-    const real* hiY = SY ? I.psiH[0][1] : nullptr;
-    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
-    real* hoX = SX ? I.psiH[1][0] : nullptr;
-    real* hoY = SY ? I.psiH[1][1] : nullptr;
-    real* hoZ = SZ ? I.psiH[1][2] : nullptr;
-    real* peX = SX ? I.psiE[0] : nullptr;
-    real* peY = SY ? I.psiE[1] : nullptr;
-    real* peZ = SZ ? I.psiE[2] : nullptr;
+    // psi bases moved by qf: with the field offsets (which include qf) they
+    // reach group member blockIdx.y's psi at + 2 qf
+    const real* hiX = SX ? I.psiH[0][0] + qf : nullptr;
+    const real* hiY = SY ? I.psiH[0][1] + qf : nullptr;
+    const real* hiZ = SZ ? I.psiH[0][2] + qf : nullptr;
+    real* hoX = SX ? I.psiH[1][0] + qf : nullptr;
+    real* hoY = SY ? I.psiH[1][1] + qf : nullptr;
+    real* hoZ = SZ ? I.psiH[1][2] + qf : nullptr;
+    real* peX = SX ? I.psiE[0] + qf : nullptr;
+    real* peY = SY ? I.psiE[1] + qf : nullptr;
+    real* peZ = SZ ? I.psiE[2] + qf : nullptr;
     const real S = I.S;
 
     const bool xm = !EDGE || i > 0, xp1 = !EDGE || i + 2 < nx;
@@ -853,7 +864,7 @@ __device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty
     }
 
     int k = z0 > 0 ? z0 - 1 : 0;
-    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i + qf;  // group member blockIdx.y
     V2 ex_c = ld2(eX, o), ey_c = ld2(eY, o), eym_c = ld2z(eY, o - px, ym);
     real exm_c = hm ? ldg(eX, o - 1) : real(0);
     V2 hxp, hyp;
@@ -863,7 +874,7 @@ __device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty
     const int i0 = tx * LX;
     const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
     // a half-warp's 16 lanes take rows 0-15: the z psi rows (SZ) go without
-    volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, lane, xt, yo));
+    volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, lane, xt, yo, qf));
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;
@@ -1111,30 +1122,22 @@ __global__ void __launch_bounds__(LX * LY, plain_minb<real>())
 k_lean_plain(const __grid_constant__ LeanTable<real> tab) {
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    const unsigned qf = blockIdx.y * tab.qvol;
     if (tile_edge(tab.inst, tx, ty, tz, ZB))
-        plain_block<real, ZB, true>(tab.inst, tx, ty, tz);
+        plain_block<real, ZB, true>(tab.inst, tx, ty, tz, qf);
     else
-        plain_block<real, ZB, false>(tab.inst, tx, ty, tz);
-}
-
-template <typename real, int ZB, int MASK, bool EXTRAS>
-__device__ __forceinline__ void tile_block_any(const InstDev<real>& I, int tx, int ty, int tz, long long n,
-                                               bool dry) {
-    if (tile_edge(I, tx, ty, tz, ZB))
-        tile_block<real, ZB, MASK, EXTRAS, true>(I, tx, ty, tz, n, dry);
-    else
-        tile_block<real, ZB, MASK, EXTRAS, false>(I, tx, ty, tz, n, dry);
+        plain_block<real, ZB, false>(tab.inst, tx, ty, tz, qf);
 }
 
 // sh: the kernel's two shared planes (declared once per kernel, not per
 // instantiation of the body)
 template <typename real, int ZB, int MASK>
 __device__ __forceinline__ void tile_halo_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
-                                              HaloPlane<real>* sh) {
+                                              HaloPlane<real>* sh, unsigned qf) {
     if (tile_edge(I, tx, ty, tz, ZB))
-        tile_halo<real, ZB, MASK, true>(I, tx, ty, tz, dry, sh);
+        tile_halo<real, ZB, MASK, true>(I, tx, ty, tz, dry, sh, qf);
     else
-        tile_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh);
+        tile_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh, qf);
 }
 
 // Single-slab tiles: the footprint touches the slabs of exactly one axis.
@@ -1144,12 +1147,13 @@ k_lean_slab(const __grid_constant__ LeanTable<real> tab) {
     __shared__ HaloPlane<real> sh[2];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 1)
-        tile_halo_any<real, ZB, 1>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 1>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 2)
-        tile_halo_any<real, ZB, 2>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 2>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else
-        tile_halo_any<real, ZB, 4>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 4>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
 }
 
 // Multi-slab tiles: the slabs of two or three axes (edges and corners).
@@ -1159,14 +1163,15 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
     __shared__ HaloPlane<real> sh[2];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 3)
-        tile_halo_any<real, ZB, 3>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 3>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 5)
-        tile_halo_any<real, ZB, 5>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 5>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 6)
-        tile_halo_any<real, ZB, 6>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 6>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else
-        tile_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh);
+        tile_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
 }
 
 // Plain tiles with two columns per thread (instances whose nx is a multiple
@@ -1174,11 +1179,12 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
 // thread: their two-column bodies need too many registers for the occupancy
 // the kernels live on.)
 template <typename real, int ZB, int MASK>
-__device__ __forceinline__ void tile_pair_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry) {
+__device__ __forceinline__ void tile_pair_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
+                                              unsigned qf) {
     if (tile_edge(I, tx, ty, tz, ZB))
-        tile_pair<real, ZB, MASK, true>(I, tx, ty, tz, dry);
+        tile_pair<real, ZB, MASK, true>(I, tx, ty, tz, dry, qf);
     else
-        tile_pair<real, ZB, MASK, false>(I, tx, ty, tz, dry);
+        tile_pair<real, ZB, MASK, false>(I, tx, ty, tz, dry, qf);
 }
 
 template <typename real, int ZB>
@@ -1186,7 +1192,7 @@ __global__ void __launch_bounds__(LX * LY / 2, pair_plain_minb<real>())
 k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
-    tile_pair_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0);
+    tile_pair_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, blockIdx.y * tab.qvol);
 }
 
 // General tiles (a source or dispersive voxel in the footprint), then the
@@ -1321,18 +1327,21 @@ long long general_blocks(const InstDev<real>& I, const LeanTiles& T, int q, int 
 }  // namespace
 
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanFix& fix, int n_inst) {
+int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanGroup* groups, int n_groups,
+                  const LeanFix& fix, int n_inst) {
     int total = 0;
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) total += fix.count[p] > 0;
-    for (int q = 0; q < n_inst; ++q) {
+    for (int g = 0; g < n_groups; ++g)
         for (int c = 0; c < LEAN_CLASSES; ++c)
-            if (c != LEAN_GENERAL && tiles[q].count[c] > 0) ++total;
+            if (c != LEAN_GENERAL && tiles[groups[g].lead].count[c] > 0) ++total;
+    for (int q = 0; q < n_inst; ++q)
         if (general_blocks(h_insts[q], tiles[q], q, 0) > 0) ++total;
-    }
     return total;
 }
-template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, const LeanFix&, int);
-template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, const LeanFix&, int);
+template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, const LeanGroup*, int, const LeanFix&,
+                                  int);
+template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, const LeanGroup*, int, const LeanFix&,
+                                   int);
 
 template <typename real>
 void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes) {
@@ -1357,11 +1366,11 @@ template void lean_fix_blocks<double>(const InstDev<double>*, int, std::vector<i
 // as there are instances are forked.
 template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
-                             const LeanFix& fix, int n_inst, int zb, int dry, int cur, DevState* st,
-                             const LeanStreams& ls) {
+                             const LeanGroup* groups, int n_groups, const LeanFix& fix, int n_inst, int zb, int dry,
+                             int cur, DevState* st, const LeanStreams& ls) {
     cudaError_t e = cudaSuccess;
     const bool fork = ls.side[0] != nullptr;
-    const int nsets = fork ? std::min(n_inst, LEAN_SETS) : 0;
+    const int nsets = fork ? std::min(std::max(n_inst, n_groups), LEAN_SETS) : 0;
     if (fork) {
         e = cudaEventRecord(ls.fork, ls.main);
         for (int q = 0; q < nsets * LEAN_CLASSES && e == cudaSuccess; ++q)
@@ -1372,7 +1381,8 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
     const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS);
-    for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
+    // descriptor of instance q with the step's parity applied
+    auto table = [&](int q) {
         LeanTable<real> t;
         t.inst = h_insts[q];
         if (cur) {
@@ -1381,23 +1391,31 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         }
         t.dry = dry;
         t.step_blocks = (unsigned)gtotal;
-        const LeanTiles& T = tiles[q];
-        const long long gb = general_blocks(h_insts[q], T, q, dry);
-        const bool pairs = h_insts[q].nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
+        t.qvol = (unsigned)h_insts[q].vol;
+        return t;
+    };
+    auto set_streams = [&](int s, cudaStream_t* sc) {
+        for (int c = 0; c < LEAN_CLASSES; ++c) sc[c] = fork ? ls.side[(s % LEAN_SETS) * LEAN_CLASSES + c] : ls.main;
+    };
+    // plain, slab and multi tiles: one launch per group and class, blockIdx.y = member
+    for (int g = 0; g < n_groups && e == cudaSuccess; ++g) {
+        LeanTable<real> t = table(groups[g].lead);
+        const LeanTiles& T = tiles[groups[g].lead];
+        const unsigned gn = (unsigned)groups[g].n;
+        const bool pairs = t.inst.nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
         cudaStream_t sc[LEAN_CLASSES];
-        for (int c = 0; c < LEAN_CLASSES; ++c)
-            sc[c] = fork ? ls.side[(q % LEAN_SETS) * LEAN_CLASSES + c] : ls.main;
+        set_streams(g, sc);
 #define SJ_ZB(Z)                                                                                             \
     case Z:                                                                                                  \
         t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
-        if (t.n_tiles) k_lean_multi<real, Z><<<(unsigned)t.n_tiles, halo, 0, sc[LEAN_MULTI]>>>(t);           \
+        if (t.n_tiles) k_lean_multi<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_MULTI]>>>(t); \
         t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
-        if (t.n_tiles) k_lean_slab<real, Z><<<(unsigned)t.n_tiles, halo, 0, sc[LEAN_SLAB]>>>(t);             \
-        t.tiles = T.list[LEAN_GENERAL], t.n_tiles = T.count[LEAN_GENERAL];                                   \
-        if (gb) k_lean_general<real, Z><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st);                \
+        if (t.n_tiles) k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);   \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
-        if (t.n_tiles && pairs) k_lean_plain2<real, Z><<<(unsigned)t.n_tiles, half, 0, sc[LEAN_PLAIN]>>>(t); \
-        if (t.n_tiles && !pairs) k_lean_plain<real, Z><<<(unsigned)t.n_tiles, block, 0, sc[LEAN_PLAIN]>>>(t); \
+        if (t.n_tiles && pairs)                                                                              \
+            k_lean_plain2<real, Z><<<dim3((unsigned)t.n_tiles, gn), half, 0, sc[LEAN_PLAIN]>>>(t);           \
+        if (t.n_tiles && !pairs)                                                                             \
+            k_lean_plain<real, Z><<<dim3((unsigned)t.n_tiles, gn), block, 0, sc[LEAN_PLAIN]>>>(t);           \
         break;
         switch (zb) {  // z-segment length
             SJ_ZB(8)
@@ -1406,6 +1424,22 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
             default: return cudaErrorInvalidValue;
         }
 #undef SJ_ZB
+        e = cudaGetLastError();
+    }
+    // general tiles (H sources) and probe blocks: one launch per instance
+    for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
+        const long long gb = general_blocks(h_insts[q], tiles[q], q, dry);
+        if (!gb) continue;
+        LeanTable<real> t = table(q);
+        t.tiles = tiles[q].list[LEAN_GENERAL], t.n_tiles = tiles[q].count[LEAN_GENERAL];
+        cudaStream_t sc[LEAN_CLASSES];
+        set_streams(q, sc);
+        switch (zb) {
+            case 8: k_lean_general<real, 8><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
+            case 16: k_lean_general<real, 16><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
+            case 32: k_lean_general<real, 32><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
+            default: return cudaErrorInvalidValue;
+        }
         e = cudaGetLastError();
     }
     if (fork) {
@@ -1427,7 +1461,9 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 }
 
 template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*, const LeanTiles*,
-                                              const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
+                                              const LeanGroup*, int, const LeanFix&, int, int, int, int, DevState*,
+                                              const LeanStreams&);
 template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const LeanTiles*,
-                                             const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
+                                             const LeanGroup*, int, const LeanFix&, int, int, int, int, DevState*,
+                                             const LeanStreams&);
 }  // namespace sj

@@ -201,6 +201,33 @@ def test_fused_plain_tiles_match_oracle(lib, oracle_lib, pml_um):
     assert rel(f.dft(), o.dft()) <= TOL64
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_grouped_launches_equal_single_runs(lib, precision):
+    # instances with the same grid and CPML (here: three 64^3 and two 48^3
+    # junctions with different pulse phases and amplitudes, interleaved
+    # with a 40^3 one) share the fused schedule's tile launches, their
+    # arrays packed at fixed strides; every instance must come out bit for
+    # bit as it does alone (64^3: two-column plain tiles; 48^3 and 40^3:
+    # one-column plain tiles and partial edge tiles)
+    shapes = [(64, 20.0, 0.3, 2.0), (48, 15.0, 1.1, 0.7), (64, 20.0, 2.9, 0.2), (40, 12.5, 0.5, 1.0),
+              (48, 15.0, 5.0, 3.0), (64, 20.0, 4.4, 1.3)]
+    insts = [junction_instance(n=n, res=r, phase=ph, amplitude=a, probe_components=("Ex", "Ez"))
+             for (n, r, ph, a) in shapes]
+    f = Fields(insts, precision, "fused")
+    f.autotune(2)
+    singles = [Fields(i, precision, "fused") for i in insts]
+    assert f.launches_per_step() < sum(s.launches_per_step() for s in singles)
+    f.step(120)
+    for q, s in enumerate(singles):
+        s.set_tiling(*f.tiling())
+        s.step(120)
+        for c in range(6):
+            np.testing.assert_array_equal(f.get_array(c, q), s.get_array(c), err_msg=f"instance {q} component {c}")
+        np.testing.assert_array_equal(f.monitors(q), s.monitors())
+        np.testing.assert_array_equal(f.dft(q), s.dft())
+        s.close()
+
+
 @pytest.mark.parametrize("schedule", ["fused", "tma"])
 def test_autotune_leaves_state_untouched(lib, schedule):
     inst = junction_instance(n=40, res=12.5)
