@@ -159,6 +159,9 @@ struct sj_sim {
     std::vector<std::vector<int>> lmembers;  // per group: its instances, member order
     void* d_fix = nullptr;             // correction block tables (E sources, polarisations)
     LeanFix lfix{};
+    void* d_gen = nullptr;             // general-launch block table
+    LeanGen lgen{};
+    void* d_parity = nullptr;          // every instance descriptor twice, by parity (LeanGen)
     cudaStream_t side[LEAN_STREAMS] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[LEAN_STREAMS] = {};
     // bumped whenever a descriptor changes; a graph holding parameter copies
@@ -642,6 +645,19 @@ void upload_table(sj_sim* sim) {
     ck(cudaStreamSynchronize(sim->stream), "sync before table upload");
     ck(cudaMemcpy(sim->d_table, buf.data(), buf.size(), cudaMemcpyHostToDevice), "table upload");
     sim->h2d += (long long)buf.size();
+    // by parity: entry cur * n + q has slot 0 = buffer cur (fields, H-side psi)
+    std::vector<InstDev<real>> par(2 * (size_t)n);
+    for (int q = 0; q < n; ++q) {
+        par[q] = dv[q];
+        InstDev<real>& t = par[n + q];
+        t = dv[q];
+        for (int c = 0; c < 6; ++c) std::swap(t.F[0][c], t.F[1][c]);
+        for (int a = 0; a < 3; ++a) std::swap(t.psiH[0][a], t.psiH[1][a]);
+    }
+    if (!sim->d_parity) sim->d_parity = sim->dalloc(par.size() * sizeof(InstDev<real>), false);
+    ck(cudaMemcpy(sim->d_parity, par.data(), par.size() * sizeof(InstDev<real>), cudaMemcpyHostToDevice),
+       "parity table upload");
+    sim->h2d += (long long)(par.size() * sizeof(InstDev<real>));
     sim->table_version += 1;
 }
 
@@ -787,6 +803,7 @@ void prepare_lean(sj_sim* sim) {
     std::vector<unsigned> all;
     std::vector<long long> off((size_t)sim->n_inst * LEAN_CLASSES);
     std::vector<unsigned> lists[LEAN_CLASSES];
+    std::vector<std::vector<unsigned>> general(sim->n_inst);
     sim->ltiles.assign(sim->n_inst, LeanTiles{});
     for (int q = 0; q < sim->n_inst; ++q) {
         if (2 * dv[q].vol >= (1LL << 32))
@@ -798,6 +815,7 @@ void prepare_lean(sj_sim* sim) {
             sim->ltiles[q].count[c] = (long long)lists[c].size();
             all.insert(all.end(), lists[c].begin(), lists[c].end());
         }
+        general[q] = lists[LEAN_GENERAL];
     }
     // a group's launches use the lead's lists: its members' must be equal
     for (const auto& mem : sim->lmembers)
@@ -815,6 +833,13 @@ void prepare_lean(sj_sim* sim) {
     for (int q = 0; q < sim->n_inst; ++q)
         for (int c = 0; c < LEAN_CLASSES; ++c)
             sim->ltiles[q].list[c] = base + off[(size_t)q * LEAN_CLASSES + c];
+    // the general launch's blocks
+    std::vector<int4> gblk;
+    lean_gen_blocks<real>(dv.data(), general.data(), sim->n_inst, gblk, sim->lgen.n_tiles);
+    sim->lgen.n_all = (long long)gblk.size();
+    sim->dfree(sim->d_gen);
+    sim->d_gen = sim->upload(gblk);
+    sim->lgen.blk = reinterpret_cast<const int4*>(sim->d_gen);
     // correction passes (independent of the tiling)
     std::vector<int2> passes[LEAN_FIX_PASSES];
     lean_fix_blocks<real>(dv.data(), sim->n_inst, passes);
@@ -854,6 +879,11 @@ LeanStreams lean_streams(sj_sim* sim) {
     return ls;
 }
 
+template <typename real>
+const InstDev<real>* parity_table(sj_sim* sim) {
+    return reinterpret_cast<const InstDev<real>*>(sim->d_parity);
+}
+
 // One step.  The single-pass schedules alternate the ping-pong buffers; the
 // host mirror of the parity (sim->cur) flips with every launched step.
 template <typename real>
@@ -863,8 +893,9 @@ cudaError_t launch_one(sj_sim* sim) {
     cudaError_t e;
     if (sim->schedule == SJ_SCHED_FUSED) {
         prepare_lean<real>(sim);
-        e = launch_lean_step<real>(dv.data(), d, sim->ltiles.data(), sim->lgroups.data(), (int)sim->lgroups.size(),
-                                   sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur, sim->d_state, lean_streams(sim));
+        e = launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), sim->ltiles.data(), sim->lgroups.data(),
+                                   (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur,
+                                   sim->d_state, lean_streams(sim));
     } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
@@ -894,13 +925,15 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
         prepare_lean<real>(sim);
         const LeanTiles* lt = sim->ltiles.data();
         const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
-        ck(launch_lean_step<real>(dv.data(), d, lt, sim->lgroups.data(), (int)sim->lgroups.size(), sim->lfix,
-                                  sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+        ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
+                                  (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
+                                  sim->d_state, ls),
            "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
-            ck(launch_lean_step<real>(dv.data(), d, lt, sim->lgroups.data(), (int)sim->lgroups.size(), sim->lfix,
-                                      sim->n_inst, zb, 1, sim->cur, sim->d_state, ls),
+            ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
+                                      (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
+                                      sim->d_state, ls),
                "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
@@ -1677,8 +1710,7 @@ int32_t sj_launches_per_step(const sj_sim* sim) {
         for (int p = 0; p < LEAN_FIX_PASSES; ++p) fx.count[p] = (long long)passes[p].size();
         const LeanGroup* lg = sim->lgroups.data();
         const int ng = (int)sim->lgroups.size();
-        return sim->precision == SJ_F64 ? lean_launches(sim->h64.data(), lt.data(), lg, ng, fx, sim->n_inst)
-                                        : lean_launches(sim->h32.data(), lt.data(), lg, ng, fx, sim->n_inst);
+        return lean_launches(lt.data(), lg, ng, fx);
     }
     if (sim->schedule == SJ_SCHED_TMA) return 1;
     int maxp = 0;

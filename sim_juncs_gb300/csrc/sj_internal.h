@@ -158,9 +158,19 @@ struct LeanFix {
 };
 template <typename real>
 void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes);
+// The general launch of a step: one block per H-source tile and per probe
+// block of every instance.  blk[b] = (instance, 0, tile code) or (instance,
+// 1, probe chunk); the tiles come first, so a dry launch takes the first
+// n_tiles entries.  Descriptors come from a device table holding every
+// instance twice, by parity (entry cur * n_inst + q has slot 0 = buffer cur).
+struct LeanGen {
+    const int4* blk;
+    long long n_tiles, n_all;
+};
 template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanGroup* groups, int n_groups,
-                  const LeanFix& fix, int n_inst);
+void lean_gen_blocks(const InstDev<real>* h_insts, const std::vector<unsigned>* general_tiles, int n_inst,
+                     std::vector<int4>& blk, long long& n_tiles);
+int lean_launches(const LeanTiles* tiles, const LeanGroup* groups, int n_groups, const LeanFix& fix);
 // Streams of one fused step: LEAN_SETS sets of one stream per tile class,
 // forked from `main` and joined back into it with the events; group g's
 // launches go to set g % LEAN_SETS (instance q's general launch to set
@@ -174,8 +184,9 @@ struct LeanStreams {
     cudaEvent_t fork, join[LEAN_STREAMS];
 };
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
-                             const LeanGroup* groups, int n_groups, const LeanFix& fix, int n_inst, int zb, int dry,
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
+                             const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
+                             int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
                              int cur, DevState* st, const LeanStreams& ls);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)

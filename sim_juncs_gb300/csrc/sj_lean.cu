@@ -67,7 +67,7 @@ constexpr int LMAXF = 256;
 #define SJ_LEAN_MULTI_MINB 3
 #endif
 #ifndef SJ_LEAN_GEN_MINB
-#define SJ_LEAN_GEN_MINB 4
+#define SJ_LEAN_GEN_MINB 2
 #endif
 template <typename real>
 constexpr int plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PLAIN_MINB : 3; }
@@ -80,7 +80,7 @@ constexpr int slab_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB_MINB : 2; }
 template <typename real>
 constexpr int multi_minb() { return sizeof(real) == 4 ? SJ_LEAN_MULTI_MINB : 2; }
 template <typename real>
-constexpr int general_minb() { return sizeof(real) == 4 ? SJ_LEAN_GEN_MINB : 2; }
+constexpr int general_minb() { return sizeof(real) == 4 ? SJ_LEAN_GEN_MINB : 1; }
 
 // Reads of buffer `cur` (fields, H-side psi), profiles and material tables
 // go through the non-coherent path: nothing writes them during the step, and
@@ -1195,23 +1195,28 @@ k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
     tile_pair_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, blockIdx.y * tab.qvol);
 }
 
-// General tiles (a source or dispersive voxel in the footprint), then the
-// probe blocks.
+// General tiles (an H source in the footprint) and probe blocks of every
+// instance, one launch per step (LeanGen).
 template <typename real, int ZB>
 __global__ void __launch_bounds__(LX * LY, general_minb<real>())
-k_lean_general(const __grid_constant__ LeanTable<real> tab, DevState* st) {
+k_lean_general(const InstDev<real>* __restrict__ parity_tab, const int4* __restrict__ blk, long long n_blk,
+               int n_inst, int cur, int dry, unsigned step_blocks, DevState* st) {
     const long long n = st->step;
     const long long b = blockIdx.x;
-    if (b < tab.n_tiles) {
-        int tx, ty, tz, m;
-        tile_decode(__ldg(tab.tiles + b), tx, ty, tz, m);
-        // tile_block returns early for columns outside the grid; every
-        // thread still reaches the barrier in finish_block
-        tile_block<real, ZB, 7, true, true>(tab.inst, tx, ty, tz, n, tab.dry != 0);
-    } else if (!tab.dry) {
-        lean_probe_block<real>(tab.inst, b - tab.n_tiles, n, 0, st);
+    if (b < n_blk) {  // beyond: the one counting block of a step without general work
+        const int4 e = blk[b];
+        const InstDev<real>& I = parity_tab[(long long)cur * n_inst + e.x];
+        if (e.y == 0) {
+            int tx, ty, tz, m;
+            tile_decode((unsigned)e.z, tx, ty, tz, m);
+            // tile_block returns early for columns outside the grid; every
+            // thread still reaches the barrier in finish_block
+            tile_block<real, ZB, 7, true, true>(I, tx, ty, tz, n, dry != 0);
+        } else if (!dry) {
+            lean_probe_block<real>(I, e.z, n, 0, st);
+        }
     }
-    finish_block(tab.step_blocks, tab.dry, st);
+    finish_block(step_blocks, dry, st);
 }
 
 // ------------------------------------------------------------ corrections
@@ -1316,32 +1321,36 @@ long long probe_blocks(const InstDev<real>& I) {
     return (I.n_probe + LX * LY - 1) / (LX * LY);
 }
 
-// blocks of instance q's general launch (the first instance's always has
-// at least one, so that every step has a block that advances the counter)
-template <typename real>
-long long general_blocks(const InstDev<real>& I, const LeanTiles& T, int q, int dry) {
-    const long long g = T.count[LEAN_GENERAL] + (dry ? 0 : probe_blocks(I));
-    return (q == 0 && g == 0) ? 1 : g;
+// blocks of the step's general launch (at least one, so that every step
+// has a block that advances the counter)
+long long general_blocks(const LeanGen& gen, int dry) {
+    return std::max(1LL, dry ? gen.n_tiles : gen.n_all);
 }
 
 }  // namespace
 
-template <typename real>
-int lean_launches(const InstDev<real>* h_insts, const LeanTiles* tiles, const LeanGroup* groups, int n_groups,
-                  const LeanFix& fix, int n_inst) {
-    int total = 0;
+int lean_launches(const LeanTiles* tiles, const LeanGroup* groups, int n_groups, const LeanFix& fix) {
+    int total = 1;  // the general launch
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) total += fix.count[p] > 0;
     for (int g = 0; g < n_groups; ++g)
         for (int c = 0; c < LEAN_CLASSES; ++c)
             if (c != LEAN_GENERAL && tiles[groups[g].lead].count[c] > 0) ++total;
-    for (int q = 0; q < n_inst; ++q)
-        if (general_blocks(h_insts[q], tiles[q], q, 0) > 0) ++total;
     return total;
 }
-template int lean_launches<float>(const InstDev<float>*, const LeanTiles*, const LeanGroup*, int, const LeanFix&,
-                                  int);
-template int lean_launches<double>(const InstDev<double>*, const LeanTiles*, const LeanGroup*, int, const LeanFix&,
-                                   int);
+template <typename real>
+void lean_gen_blocks(const InstDev<real>* h_insts, const std::vector<unsigned>* general_tiles, int n_inst,
+                     std::vector<int4>& blk, long long& n_tiles) {
+    blk.clear();
+    for (int q = 0; q < n_inst; ++q)
+        for (unsigned code : general_tiles[q]) blk.push_back(make_int4(q, 0, (int)code, 0));
+    n_tiles = (long long)blk.size();
+    for (int q = 0; q < n_inst; ++q)
+        for (long long c = 0; c < probe_blocks(h_insts[q]); ++c) blk.push_back(make_int4(q, 1, (int)c, 0));
+}
+template void lean_gen_blocks<float>(const InstDev<float>*, const std::vector<unsigned>*, int, std::vector<int4>&,
+                                     long long&);
+template void lean_gen_blocks<double>(const InstDev<double>*, const std::vector<unsigned>*, int,
+                                      std::vector<int4>&, long long&);
 
 template <typename real>
 void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>* passes) {
@@ -1365,20 +1374,21 @@ template void lean_fix_blocks<double>(const InstDev<double>*, int, std::vector<i
 // kernels of a step overlap and fill each other's tails.  Only as many sets
 // as there are instances are forked.
 template <typename real>
-cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts, const LeanTiles* tiles,
-                             const LeanGroup* groups, int n_groups, const LeanFix& fix, int n_inst, int zb, int dry,
+cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
+                             const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
+                             int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
                              int cur, DevState* st, const LeanStreams& ls) {
     cudaError_t e = cudaSuccess;
     const bool fork = ls.side[0] != nullptr;
-    const int nsets = fork ? std::min(std::max(n_inst, n_groups), LEAN_SETS) : 0;
+    const int nsets = fork ? std::min(std::max(n_groups, 1), LEAN_SETS) : 0;
     if (fork) {
         e = cudaEventRecord(ls.fork, ls.main);
         for (int q = 0; q < nsets * LEAN_CLASSES && e == cudaSuccess; ++q)
             e = cudaStreamWaitEvent(ls.side[q], ls.fork, 0);
         if (e != cudaSuccess) return e;
     }
-    long long gtotal = 0;
-    for (int q = 0; q < n_inst; ++q) gtotal += general_blocks(h_insts[q], tiles[q], q, dry);
+    const long long gb = general_blocks(gen, dry);
+    long long gtotal = gb;
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
     const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS);
     // descriptor of instance q with the step's parity applied
@@ -1426,18 +1436,21 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 #undef SJ_ZB
         e = cudaGetLastError();
     }
-    // general tiles (H sources) and probe blocks: one launch per instance
-    for (int q = 0; q < n_inst && e == cudaSuccess; ++q) {
-        const long long gb = general_blocks(h_insts[q], tiles[q], q, dry);
-        if (!gb) continue;
-        LeanTable<real> t = table(q);
-        t.tiles = tiles[q].list[LEAN_GENERAL], t.n_tiles = tiles[q].count[LEAN_GENERAL];
+    // general tiles (H sources) and probe blocks of all instances: one launch
+    if (e == cudaSuccess) {
         cudaStream_t sc[LEAN_CLASSES];
-        set_streams(q, sc);
+        set_streams(0, sc);
+        const long long nb = dry ? gen.n_tiles : gen.n_all;
         switch (zb) {
-            case 8: k_lean_general<real, 8><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
-            case 16: k_lean_general<real, 16><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
-            case 32: k_lean_general<real, 32><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(t, st); break;
+#define SJ_GEN(Z)                                                                                       \
+    case Z:                                                                                             \
+        k_lean_general<real, Z><<<(unsigned)gb, block, 0, sc[LEAN_GENERAL]>>>(d_parity, gen.blk, nb, n_inst, \
+                                                                             cur, dry, (unsigned)gtotal, st); \
+        break;
+            SJ_GEN(8)
+            SJ_GEN(16)
+            SJ_GEN(32)
+#undef SJ_GEN
             default: return cudaErrorInvalidValue;
         }
         e = cudaGetLastError();
@@ -1460,10 +1473,11 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     return e;
 }
 
-template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*, const LeanTiles*,
-                                              const LeanGroup*, int, const LeanFix&, int, int, int, int, DevState*,
+template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*,
+                                              const InstDev<double>*, const LeanTiles*, const LeanGroup*, int,
+                                              const LeanGen&, const LeanFix&, int, int, int, int, DevState*,
                                               const LeanStreams&);
-template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const LeanTiles*,
-                                             const LeanGroup*, int, const LeanFix&, int, int, int, int, DevState*,
-                                             const LeanStreams&);
+template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const InstDev<float>*,
+                                             const LeanTiles*, const LeanGroup*, int, const LeanGen&,
+                                             const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
 }  // namespace sj
