@@ -202,7 +202,8 @@ def run_ours(args):
     value = voxels * args.steps * ws / secs
     peak, peak_kind = measured_peak()
     achieved = bytes_step / (secs / args.steps) / 1e9
-    kernel = {"fused": "fused step: general, single-slab and plain column-march kernels, concurrent",
+    kernel = {"fused": "fused step: plain, slab and multi tile launches per instance group and one general "
+                       "launch, concurrent (one HBM pass)",
               "tma": "k_fused (TMA shared-memory tiles), one launch per step",
               "split": "k_split_h + k_split_e"}[schedule]
     out = {
@@ -222,6 +223,7 @@ def run_ours(args):
 
     if rank == 0 and not args.no_extras:
         out["fp64_plain"] = fp64_leg(torch, args)
+        out["fp64_same_workload"] = fp64_same_workload(torch, args, insts, value / ws)
         out["fp32_vs_fp64"] = error_leg(schedule)
     if rank == 0:
         out["e2e"] = e2e_leg(args, insts, schedule, til)
@@ -262,6 +264,35 @@ def fp64_leg(torch, args):
            "ms_per_step": secs / steps * 1e3, "steps": steps, "gpu_launches": launches,
            "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "peak_kind": kind, "algorithmic_bytes_per_step": b}}
+    f.close()
+    return res
+
+
+def fp64_same_workload(torch, args, insts, fp32_value):
+    """FP64 (the library's default schedule) on the headline workload itself:
+    plain = one instance at a time (each distinct grid timed alone, weighted
+    by how many instances share it), batched = all instances in one
+    simulation.  fp32_over_fp64_* = the FP32 headline value over each."""
+    from sim_juncs_gb300.fields import Fields
+    steps = max(3, args.steps // 8)
+    shapes = {}
+    for inst in insts:
+        g = inst.grid
+        shapes.setdefault((g.nx, g.ny, g.nz, g.dx), []).append(inst)
+    total_vox, total_s = 0, 0.0
+    for members in shapes.values():
+        f = Fields(members[0], "f64", stream=torch.cuda.current_stream())
+        secs, _ = time_steps(f, torch, steps, 2)
+        total_vox += len(members) * f.voxels() * steps
+        total_s += len(members) * secs
+        f.close()
+    plain = total_vox / total_s
+    f = Fields(insts, "f64", stream=torch.cuda.current_stream())
+    secs, launches = time_steps(f, torch, steps, 2)
+    batched = f.voxels() * steps / secs
+    res = {"schedule": f.schedule_name(), "unit": UNIT, "steps": steps,
+           "plain_value": plain, "batched_value": batched, "batched_gpu_launches": launches,
+           "fp32_over_fp64_plain": fp32_value / plain, "fp32_over_fp64_batched": fp32_value / batched}
     f.close()
     return res
 

@@ -61,12 +61,13 @@ enum { SJ_EX = 0, SJ_EY = 1, SJ_EZ = 2, SJ_HX = 3, SJ_HY = 4, SJ_HZ = 5 };
    monitor sums are always FP64 */
 enum { SJ_F64 = 0, SJ_F32 = 1 };
 
-/* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel (one thread
-   per (i,j) column marching z, neighbour H recomputed, no shared memory);
-   SPLIT the two-pass (H then E) schedule; TMA the single-pass kernel that
-   stages tiles through a TMA/mbarrier shared-memory ring.  Default: FUSED for
-   SJ_F32 (HBM-bound), SPLIT for SJ_F64 (bound by FP64 arithmetic, where SPLIT
-   does the fewest operations) */
+/* kernel schedule: FUSED is the single-HBM-pass leapfrog kernel (tiles of
+   (i,j) columns marching z, neighbour H passed between warps or recomputed,
+   instances with equal grids sharing launches); SPLIT the two-pass (H then
+   E) schedule; TMA the single-pass kernel that stages tiles through a
+   TMA/mbarrier shared-memory ring.  Default: FUSED for both precisions (the
+   fastest on GB300 for both); an instance with a design region (adjoint)
+   steps with SPLIT */
 enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1, SJ_SCHED_TMA = 2 };
 
 #define SJ_MAX_POLES 8
