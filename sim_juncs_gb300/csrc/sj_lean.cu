@@ -685,10 +685,12 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
             prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, kq < nz && k + LEAN_PF < z1,
                                     SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
         }
+        // z profile values of the plane, by select (no branch)
         real bzi = 1, czi = 0, bzh = 1, czh = 0;
-        if (zo) {
+        if (SZ) {
             const real* pr = I.prof[2];
-            bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
+            bzi = zo ? ldg(pr, k) : real(1), czi = zo ? ldg(pr, nz + k) : real(0);
+            bzh = zo ? ldg(pr, 2 * nz + k) : real(1), czh = zo ? ldg(pr, 3 * nz + k) : real(0);
         }
         // every load of the H update issued together
         const unsigned op = o + qf;
@@ -723,12 +725,10 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
             // the E update's loads go ahead of the barrier (which the
             // compiler does not move loads across): the combo's inverse
             // eps_inf and the old E-side psi of the own cell
+            // (unconditional: every warp's offset is a cell of the grid)
             const bool eo = own && act;
-            real iv0 = 0, iv1 = 0, iv2 = 0;
-            if (eo) {
-                const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
-                iv0 = ldg(cf, 0), iv1 = ldg(cf, 1), iv2 = ldg(cf, 2);
-            }
+            const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
+            const real iv0 = ldg(cf, 0), iv1 = ldg(cf, 1), iv2 = ldg(cf, 2);
             const real qY0 = psi_old<SY, false>(eo && yo, peY, op), qY1 = psi_old<SY, false>(eo && yo, peY, op + vol);
             const real qZ0 = psi_old<SZ, false>(eo && zo, peZ, op), qZ1 = psi_old<SZ, false>(eo && zo, peZ, op + vol);
             const real qX0 = psi_old<SX, false>(eo && xo, peX, op), qX1 = psi_old<SX, false>(eo && xo, peX, op + vol);
