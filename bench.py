@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="sweep", choices=["sweep", "bowtie", "junction"])
     p.add_argument("--schedule", default="auto", choices=["auto", "fused", "tma", "split"])
-    p.add_argument("--e2e-steps", type=int, default=400)
+    p.add_argument("--e2e-steps", type=int, default=None,
+                   help="steps of the end-to-end job (default: the workload's steps per run)")
     p.add_argument("--no-extras", action="store_true", help="skip the FP64 and error legs")
     return p.parse_args()
 
@@ -226,7 +227,7 @@ def run_ours(args):
         out["fp64_same_workload"] = fp64_same_workload(torch, args, insts, value / ws)
         out["fp32_vs_fp64"] = error_leg(schedule)
     if rank == 0:
-        out["e2e"] = e2e_leg(args, insts, schedule, til)
+        out["e2e"] = e2e_leg(args, insts, schedule, til, args.e2e_steps or cfg["steps_per_run"])
         out["cpu_baseline"] = cpu_baseline()
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -316,11 +317,12 @@ def error_leg(schedule):
             "dft_rel_err": float(np.max(np.abs(d32 - d64)) / np.max(np.abs(d64)))}
 
 
-def e2e_leg(args, insts, schedule, til):
+def e2e_leg(args, insts, schedule, til, steps):
     """Whole job through the public API from host descriptors: create
     (uploads the scene and the per-step source tables, rasterises on the
-    device), set the tuned tiling, e2e_steps steps, then monitors + DFT back
-    to host buffers.  Wall clock, host to host."""
+    device), set the tuned tiling, `steps` steps (by default the workload's
+    whole run), then monitors + DFT back to host buffers.  Wall clock, host
+    to host."""
     from sim_juncs_gb300.fields import Fields
     import torch
     torch.cuda.synchronize()
@@ -328,15 +330,15 @@ def e2e_leg(args, insts, schedule, til):
     f = Fields(insts, "f32", schedule)
     if til is not None:
         f.set_tiling(*til)
-    f.step(args.e2e_steps)
+    f.step(steps)
     outs = [(f.monitors(q), f.dft(q)) for q in range(f.n_instances)]
     t1 = time.perf_counter()
     voxels = f.voxels()
     h2d, d2h = f.transfer_bytes()
     f.close()
-    return {"value": voxels * args.e2e_steps / (t1 - t0), "unit": UNIT,
-            "steps": args.e2e_steps, "seconds": t1 - t0,
-            "h2d_bytes_per_step": h2d / args.e2e_steps, "d2h_bytes_per_step": d2h / args.e2e_steps,
+    return {"value": voxels * steps / (t1 - t0), "unit": UNIT,
+            "steps": steps, "seconds": t1 - t0,
+            "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
             "includes": "create + device rasterise + steps + monitor/DFT read-back"}
 
 

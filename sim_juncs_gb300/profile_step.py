@@ -4,9 +4,10 @@
         [--schedule fused|tma|split] [--zseg Z] [--steps N]
 
 Workloads: sweep (32 x 96^3 + 32 x 128^3 + 32 x 192^3 junctions),
-junction192 (one 192^3 sweep member), bowtie (512 x 512 x 384),
-junction64 (64^3).  Prints the launches per step so that a capture can
-skip set-up launches and warm-up steps by count.
+junction192 (one 192^3 sweep member), junction192x4 (four 192^3 sweep
+members: one launch group, ~3.4 GB on the device), bowtie (512 x 512 x
+384), junction64 (64^3).  Prints the launches per step so that a capture
+can skip set-up launches and warm-up steps by count.
 """
 import argparse
 
@@ -19,6 +20,8 @@ def instances(name):
         return configs.sweep_instances()
     if name == "junction192":
         return [configs.junction_instance(n=192, res=60.0, probe_components=("Ez",), dft=False)]
+    if name == "junction192x4":
+        return [m for m in configs.sweep_instances() if m.grid.nx == 192][:4]
     if name == "bowtie":
         return [configs.bowtie_instance()]
     if name == "junction64":
