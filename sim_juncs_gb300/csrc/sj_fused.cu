@@ -37,7 +37,7 @@ constexpr int FTX = 32;
 constexpr int MAXF_FUSED = 256;
 constexpr unsigned long long WAIT_NS = 100000000ull;  // 100 ms (a healthy copy takes microseconds)
 constexpr int MAXC_SMEM = 16;       // combos whose coefficient rows are staged in shared memory
-constexpr int NCOEF_MAX = 3 + 3 * MAXP;
+constexpr int NCOEF_MAX = 6 + 3 * MAXP;
 
 // tensor-map slots of one instance
 constexpr int TM_E = 0, TM_H = 6, TM_C = 12, TM_PE = 13, TM_PH = 19, TM_COUNT = 31;

@@ -408,7 +408,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
     }
     const int nk = (int)H.keys.size();
     I.n_combos = nk;
-    I.ncoef = 3 + 3 * np;
+    I.ncoef = 6 + 3 * np;
     std::vector<real> coef((size_t)nk * I.ncoef);
     std::vector<uint8_t> cflag(nk, 0);
     for (int q = 0; q < nk; ++q) {
@@ -420,6 +420,9 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
                 coef[(size_t)q * I.ncoef + 3 + 3 * p + c] = (real)cs;
                 if (cs != 0.0) cflag[q] |= 1;
             }
+            // S eps_inf^-1, the product the fused E update scales curl H by
+            // (a product of two `real`s: the bits of the device's I.S * inv)
+            coef[(size_t)q * I.ncoef + 3 + 3 * np + c] = I.S * coef[(size_t)q * I.ncoef + c];
         }
     }
     I.coef = sim->upload(coef);

@@ -36,7 +36,7 @@ struct InstDev {
 
     // materials: one byte per voxel selects a "combo" = (class at Ex, Ey, Ez)
     const uint8_t* combo;       // [nz][ny][px]
-    const real* coef;           // [n_combos][ncoef]: inv_eps[3], then Csig[p][3]
+    const real* coef;           // [n_combos][ncoef]: inv_eps[3], Csig[p][3], then S * inv_eps[3]
     const uint8_t* cflag;       // [n_combos]: bit 0 = some pole has sigma != 0
     int n_combos, ncoef;
     int n_poles;

@@ -340,14 +340,15 @@ __device__ __forceinline__ real h_new(const InstDev<real>& I, int comp, real cv,
 
 // E^{n+1} of the own cell, Yee and CPML terms (sources and polarisations are
 // applied by k_lean_esrc and k_lean_disp after the tile kernels).
+// (S eps_inf^-1 comes from the combo's coefficient row)
 template <int CA, typename real>
 __device__ __forceinline__ real e_new(const InstDev<real>& I, const real* cf, real e_old, real cv) {
-    return fma(I.S * ldg(cf, CA), cv, e_old);
+    return fma(ldg(cf, I.ncoef - 3 + CA), cv, e_old);
 }
-// the same with the combo's inverse eps_inf already loaded
+// the same with the combo's S eps_inf^-1 already loaded
 template <typename real>
-__device__ __forceinline__ real e_new_v(const InstDev<real>& I, real inv, real e_old, real cv) {
-    return fma(I.S * inv, cv, e_old);
+__device__ __forceinline__ real e_new_v(real sinv, real e_old, real cv) {
+    return fma(sinv, cv, e_old);
 }
 
 // Slab axes a tile's footprint touches (bit a = axis a): the same footprint
@@ -723,12 +724,13 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
         }
         if (store) {
             // the E update's loads go ahead of the barrier (which the
-            // compiler does not move loads across): the combo's inverse
-            // eps_inf and the old E-side psi of the own cell
-            // (unconditional: every warp's offset is a cell of the grid)
+            // compiler does not move loads across): the combo's S eps_inf^-1
+            // and the old E-side psi of the own cell (the combo loads are
+            // unconditional: every warp's offset is a cell of the grid)
             const bool eo = own && act;
             const real* cf = I.coef + (int)__ldg(I.combo + o) * I.ncoef;
-            const real iv0 = ldg(cf, 0), iv1 = ldg(cf, 1), iv2 = ldg(cf, 2);
+            const real* sv = cf + I.ncoef - 3;  // S eps_inf^-1 per component
+            const real iv0 = ldg(sv, 0), iv1 = ldg(sv, 1), iv2 = ldg(sv, 2);
             const real qY0 = psi_old<SY, false>(eo && yo, peY, op), qY1 = psi_old<SY, false>(eo && yo, peY, op + vol);
             const real qZ0 = psi_old<SZ, false>(eo && zo, peZ, op), qZ1 = psi_old<SZ, false>(eo && zo, peZ, op + vol);
             const real qX0 = psi_old<SX, false>(eo && xo, peX, op), qX1 = psi_old<SX, false>(eo && xo, peX, op + vol);
@@ -758,21 +760,21 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
                         real cv = d1 - d2;
                         pml_term_v<SY, true>(cv, yo, byi, cyi, d1, qY0, peY, op, si);
                         pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, qZ0, peZ, op, si);
-                        oEX[o] = e_new_v(I, iv0, ex_c, cv);
+                        oEX[o] = e_new_v(iv0, ex_c, cv);
                     }
                     {
                         const real d1 = hx - hxp, d2 = hz - hz_xm;
                         real cv = d1 - d2;
                         pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, qZ1, peZ + vol, op, si);
                         pml_term_v<SX, false>(cv, xo, bxi, cxi, d2, qX0, peX, op, si);
-                        oEY[o] = e_new_v(I, iv1, ey_c, cv);
+                        oEY[o] = e_new_v(iv1, ey_c, cv);
                     }
                     {
                         const real d1 = hy - hy_xm, d2 = hx - hx_ym;
                         real cv = d1 - d2;
                         pml_term_v<SX, true>(cv, xo, bxi, cxi, d1, qX1, peX + vol, op, si);
                         pml_term_v<SY, false>(cv, yo, byi, cyi, d2, qY1, peY + vol, op, si);
-                        oEZ[o] = e_new_v(I, iv2, ez, cv);
+                        oEZ[o] = e_new_v(iv2, ez, cv);
                     }
                 }
             }
