@@ -317,6 +317,25 @@ int64_t sj_monitor_spectrum_length(const sj_sim* sim, int32_t inst);
 int sj_monitor_spectrum(sj_sim* sim, int32_t inst, double* out, size_t cap);
 /* full component array converted to FP64 (dump_raw, src/disp.cpp:732-737) */
 int sj_read_field(sj_sim* sim, int32_t inst, int32_t component, double* out, size_t cap);
+/* dump_raw streamed (src/disp.cpp:732-737, `if (dump_raw)` inside the save
+   point): every `every` steps, at the monitor rule (step n with
+   n % every == 0, before step n runs), component `component` of instance
+   `inst` is copied on the device into a dense [nz][ny][nx] staging slot and
+   from there to pinned host memory on a copy stream of its own, overlapped
+   with the steps that follow.  `depth` slots form a ring that
+   sj_take_snapshot drains oldest first.  When a snapshot falls due and every
+   slot still holds one not taken, sj_step / sj_step_graph stop before that
+   step and return SJ_E_RANGE (the steps before it are done; sj_time tells
+   where).  every = 0 switches snapshots off for the instance (pending ones
+   are dropped).  While any instance takes snapshots, sj_step_graph launches
+   step by step instead of replaying graphs. */
+int sj_set_snapshots(sj_sim* sim, int32_t inst, int32_t component, int32_t every, int32_t depth);
+/* the oldest snapshot not yet taken: waits for its copy, writes nx*ny*nz
+   doubles ([nz][ny][nx]) to out and the step it was taken before to *step;
+   *step = -1 (out untouched) when none is pending */
+int sj_take_snapshot(sj_sim* sim, int32_t inst, int64_t* step, double* out, size_t cap);
+/* snapshots in the ring not yet taken (in flight or copied); -1 on error */
+int32_t sj_snapshots_pending(const sj_sim* sim, int32_t inst);
 /* overwrite one component (initial conditions / checkpoint restore) */
 int sj_write_field(sj_sim* sim, int32_t inst, int32_t component, const double* in, size_t n);
 /* per-component class map the stepper uses: out[3][nz][ny][nx] */

@@ -119,6 +119,16 @@ struct HostInst {
     double last_source_time = 0;
 };
 
+// dump_raw snapshots of one instance: a ring of `depth` slots, each a dense
+// device staging copy and a pinned host copy of one component
+struct Snapshots {
+    int comp = -1, every = 0, depth = 0;
+    std::vector<void*> dev, host;
+    std::vector<cudaEvent_t> staged, done;  // staging copy made / host copy landed
+    std::vector<long long> step;
+    int head = 0, count = 0;                // oldest slot, slots holding a snapshot
+};
+
 }  // namespace
 
 struct sj_sim {
@@ -164,6 +174,9 @@ struct sj_sim {
     void* d_parity = nullptr;          // every instance descriptor twice, by parity (LeanGen)
     cudaStream_t side[LEAN_STREAMS] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[LEAN_STREAMS] = {};
+    // dump_raw snapshots (per instance) and the stream their host copies run on
+    std::vector<Snapshots> snaps;
+    cudaStream_t copy_stream = nullptr;
     // bumped whenever a descriptor changes; a graph holding parameter copies
     // of older descriptors is captured again
     long long table_version = 0;
@@ -171,6 +184,9 @@ struct sj_sim {
 
     ~sj_sim() {
         if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (Snapshots& S : snaps) release(S);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         for (int q = 0; q < LEAN_STREAMS; ++q) {
             if (side[q]) cudaStreamSynchronize(side[q]), cudaStreamDestroy(side[q]);
             if (ev_join[q]) cudaEventDestroy(ev_join[q]);
@@ -179,6 +195,19 @@ struct sj_sim {
         drop_graphs();
         for (void* p : allocs) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+    // frees a snapshot ring (its copies must have finished)
+    void release(Snapshots& S) {
+        for (void* h : S.host) cudaFreeHost(h);
+        for (void* d : S.dev) dfree(d);
+        for (cudaEvent_t e : S.staged) cudaEventDestroy(e);
+        for (cudaEvent_t e : S.done) cudaEventDestroy(e);
+        S = Snapshots{};
+    }
+    bool any_snapshots() const {
+        for (const Snapshots& S : snaps)
+            if (S.every > 0) return true;
+        return false;
     }
     void drop_graphs() {
         for (int p = 0; p < 2; ++p)
@@ -1014,11 +1043,48 @@ void autotune(sj_sim* sim, int steps, int* best_ty, int* best_ring, int* best_zs
     if (best_ms) *best_ms = best / steps;
 }
 
+// Start the snapshot of instance q due before step sim->t: a dense copy
+// into the next free staging slot on the stepping stream (the step after
+// next overwrites this buffer), then its host copy on the copy stream.
+template <typename real>
+void take_snapshot_async(sj_sim* sim, int q) {
+    Snapshots& S = sim->snaps[q];
+    if (S.count == S.depth)
+        fail(SJ_E_RANGE, "snapshot ring full at step " + std::to_string(sim->t) + ": take snapshots first");
+    const HostInst<real>& H = hostv<real>(sim)[q];
+    const InstDev<real>& I = devv<real>(sim)[q];
+    const int slot = (S.head + S.count) % S.depth;
+    const size_t row = (size_t)H.nx * sizeof(real);
+    ck(cudaMemcpy2DAsync(S.dev[slot], row, I.F[sim->cur][S.comp], (size_t)H.px * sizeof(real), row,
+                         (size_t)H.ny * H.nz, cudaMemcpyDeviceToDevice, sim->stream),
+       "snapshot staging copy");
+    ck(cudaEventRecord(S.staged[slot], sim->stream), "event");
+    ck(cudaStreamWaitEvent(sim->copy_stream, S.staged[slot], 0), "event wait");
+    ck(cudaMemcpyAsync(S.host[slot], S.dev[slot], row * H.ny * H.nz, cudaMemcpyDeviceToHost, sim->copy_stream),
+       "snapshot host copy");
+    ck(cudaEventRecord(S.done[slot], sim->copy_stream), "event");
+    S.step[slot] = sim->t;
+    S.count += 1;
+    sim->d2h += (long long)(row * H.ny * H.nz);
+}
+
 template <typename real>
 void do_steps(sj_sim* sim, long long n) {
     ensure_capacity<real>(sim, sim->t + n);
-    for (long long q = 0; q < n; ++q) ck(launch_one<real>(sim), "step launch");
-    sim->t += n;
+    if (!sim->any_snapshots()) {
+        for (long long q = 0; q < n; ++q) ck(launch_one<real>(sim), "step launch");
+        sim->t += n;
+        return;
+    }
+    // with snapshots: step by step, the counter current at every save point
+    for (long long q = 0; q < n; ++q) {
+        for (int i = 0; i < sim->n_inst; ++i) {
+            const Snapshots& S = sim->snaps[i];
+            if (S.every > 0 && sim->t % S.every == 0) take_snapshot_async<real>(sim, i);
+        }
+        ck(launch_one<real>(sim), "step launch");
+        sim->t += 1;
+    }
 }
 
 // Steps in graph replays of `chunk` steps.  The single-pass schedules bake
@@ -1027,6 +1093,7 @@ void do_steps(sj_sim* sim, long long n) {
 template <typename real>
 void do_steps_graph(sj_sim* sim, long long n, int chunk) {
     if (chunk < 1) fail(SJ_E_INVALID, "chunk must be >= 1");
+    if (sim->any_snapshots()) return do_steps<real>(sim, n);  // save points fall inside chunks
     ensure_capacity<real>(sim, sim->t + n);
     // everything that allocates or copies happens before the capture
     prepare_schedule<real>(sim);
@@ -1461,6 +1528,7 @@ void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
     hv.resize(n);
     dv.resize(n);
     for (int q = 0; q < n; ++q) build_instance<real>(sim, insts[q], hv[q], dv[q]);
+    sim->snaps.assign(n, Snapshots{});
     group_instances<real>(sim);
     upload_table<real>(sim);
 }
@@ -1787,6 +1855,67 @@ int sj_read_dft(sj_sim* sim, int32_t inst, double* out, size_t cap) {
     if (nd && nf) ck(cudaMemcpy(out, p, (size_t)nd * nf * sizeof(double2), cudaMemcpyDeviceToHost), "dft read");
     sim->d2h += (long long)nd * nf * sizeof(double2);
     SJ_CATCH(sim)
+}
+
+int sj_set_snapshots(sj_sim* sim, int32_t inst, int32_t comp, int32_t every, int32_t depth) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || comp < 0 || comp > 5) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    if (every < 0) fail(SJ_E_INVALID, "every must be >= 0");
+    if (every > 0 && (depth < 1 || depth > 64)) fail(SJ_E_INVALID, "depth must be in [1, 64]");
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    if (sim->copy_stream) ck(cudaStreamSynchronize(sim->copy_stream), "sync");
+    sim->release(sim->snaps[inst]);
+    if (every > 0) {
+        if (!sim->copy_stream)
+            ck(cudaStreamCreateWithFlags(&sim->copy_stream, cudaStreamNonBlocking), "copy stream");
+        const size_t bytes = (size_t)sj_voxels(sim, inst) * (sim->precision == SJ_F64 ? 8 : 4);
+        Snapshots& S = sim->snaps[inst];
+        S.comp = comp, S.every = every, S.depth = depth;
+        S.step.assign(depth, -1);
+        for (int k = 0; k < depth; ++k) {
+            void* h = nullptr;
+            cudaEvent_t a = nullptr, b = nullptr;
+            if (cudaMallocHost(&h, bytes) != cudaSuccess) {
+                sim->release(S);
+                fail(SJ_E_NOMEM, "pinned snapshot buffer of " + std::to_string(bytes) + " bytes");
+            }
+            S.host.push_back(h);
+            S.dev.push_back(sim->dalloc(bytes, false));
+            ck(cudaEventCreateWithFlags(&a, cudaEventDisableTiming), "event");
+            S.staged.push_back(a);
+            ck(cudaEventCreateWithFlags(&b, cudaEventDisableTiming), "event");
+            S.done.push_back(b);
+        }
+    }
+    SJ_CATCH(sim)
+}
+
+int sj_take_snapshot(sj_sim* sim, int32_t inst, int64_t* step, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || !step) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    Snapshots& S = sim->snaps[inst];
+    *step = -1;
+    if (S.count > 0) {
+        const size_t nv = (size_t)sj_voxels(sim, inst);
+        if (!out || nv > cap) fail(SJ_E_RANGE, "output buffer too small for the snapshot");
+        const int slot = S.head;
+        ck(cudaEventSynchronize(S.done[slot]), "snapshot wait");
+        if (sim->precision == SJ_F64) {
+            memcpy(out, S.host[slot], nv * sizeof(double));
+        } else {
+            const float* h = (const float*)S.host[slot];
+            for (size_t k = 0; k < nv; ++k) out[k] = (double)h[k];
+        }
+        *step = S.step[slot];
+        S.head = (S.head + 1) % S.depth;
+        S.count -= 1;
+    }
+    SJ_CATCH(sim)
+}
+
+int32_t sj_snapshots_pending(const sj_sim* sim, int32_t inst) {
+    if (!sim || inst < 0 || inst >= sim->n_inst) return -1;
+    return sim->snaps[inst].count;
 }
 
 int sj_read_field(sj_sim* sim, int32_t inst, int32_t comp, double* out, size_t cap) {

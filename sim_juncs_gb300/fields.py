@@ -239,6 +239,28 @@ class Fields:
                                         out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out
 
+    def set_snapshots(self, component, every, depth=2, inst=0):
+        """Stream `component` to host memory every `every` steps (dump_raw),
+        overlapped with stepping; `depth` snapshots may wait to be taken.
+        every = 0 switches it off."""
+        self._ck(self.lib.sj_set_snapshots(self.handle, inst, component, int(every), int(depth)))
+
+    def take_snapshot(self, inst=0, out=None):
+        """The oldest snapshot not yet taken as (step, [nz][ny][nx] float64),
+        or None; `out` (a C-contiguous float64 array of that shape) is
+        filled instead of a new array."""
+        g = self.instances[inst].grid
+        if out is None:
+            out = np.empty((g.nz, g.ny, g.nx), dtype=np.float64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == g.nx * g.ny * g.nz
+        step = C.c_int64(-1)
+        self._ck(self.lib.sj_take_snapshot(self.handle, inst, C.byref(step),
+                                           out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return None if step.value < 0 else (step.value, out)
+
+    def snapshots_pending(self, inst=0):
+        return int(self.lib.sj_snapshots_pending(self.handle, inst))
+
     def set_array(self, component, values, inst=0):
         v = np.ascontiguousarray(values, dtype=np.float64)
         self._ck(self.lib.sj_write_field(self.handle, inst, component,

@@ -275,3 +275,45 @@ def test_sweep_instances_build(lib):
     f = Fields(insts, "f32")
     f.step(5)
     assert f.voxels() == 96 ** 3 + 128 ** 3 + 192 ** 3
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_snapshots_equal_field_reads(lib, precision):
+    # dump_raw streamed: every snapshot is the field as sj_read_field returns
+    # it before the step it was taken at (save points n % every == 0)
+    inst = junction_instance(n=40, res=12.5)
+    a = Fields(inst, precision)
+    b = Fields(inst, precision)
+    a.set_snapshots(_abi.EX, every=7, depth=3)
+    got = []
+    for chunk in (10, 5, 11):
+        a.step(chunk)
+        while (s := a.take_snapshot()) is not None:
+            got.append(s)
+    a.step_graph(10, chunk=4)  # graph replays step one launch at a time meanwhile
+    while (s := a.take_snapshot()) is not None:
+        got.append(s)
+    assert [g[0] for g in got] == [0, 7, 14, 21, 28, 35]
+    for step, arr in got:
+        b.step(step - b.steps_done)
+        np.testing.assert_array_equal(arr, b.get_array(_abi.EX))
+    b.step(a.steps_done - b.steps_done)
+    for c in range(6):
+        np.testing.assert_array_equal(a.get_array(c), b.get_array(c))
+
+
+def test_snapshot_ring_full_stops_stepping(lib):
+    inst = junction_instance(n=32, res=10.0)
+    f = Fields(inst, "f32")
+    f.set_snapshots(_abi.EZ, every=1, depth=3)
+    with pytest.raises(_abi.SJError) as e:
+        f.step(5)
+    assert e.value.code == _abi.SJ_E_RANGE
+    assert f.steps_done == 3 and f.snapshots_pending() == 3
+    assert [f.take_snapshot()[0] for _ in range(3)] == [0, 1, 2]
+    assert f.take_snapshot() is None
+    f.step(2)
+    assert f.steps_done == 5 and f.snapshots_pending() == 2
+    f.set_snapshots(_abi.EZ, every=0)
+    f.step(3)
+    assert f.snapshots_pending() == 0 and f.steps_done == 8
