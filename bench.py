@@ -214,7 +214,8 @@ def run_ours(args):
         "config": dict(cfg, schedule=schedule, l2="state larger than L2 (no flush needed)",
                        voxels_per_step=voxels, parallelism=f"replicas{ws}"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic_per_step(schedule, voxels),
+                     "frac": achieved / peak, "frac_of_nominal_7900": achieved / 7900.0,
+                     "traffic": traffic_per_step(schedule, voxels),
                      "peak_kind": peak_kind, "algorithmic_bytes_per_step": bytes_step, "kernel": kernel},
         "gpu_launches": launches,
         "clocks": clk,
@@ -342,6 +343,27 @@ def e2e_leg(args, insts, schedule, til, steps):
             "includes": "create + device rasterise + steps + monitor/DFT read-back"}
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
 def cpu_sample():
     """Bounded CPU sample: one 96^3 sweep member, FP64 restatement."""
     from sim_juncs_gb300 import configs
@@ -362,8 +384,9 @@ def cpu_baseline(target_s=10.0):
     o.step(steps)
     secs = time.perf_counter() - t0
     return {"value": inst.grid.voxels * steps / secs, "unit": UNIT, "cores": oracle.threads(),
-            "kind": "port", "sample": f"one 96^3 sweep member, {steps} FP64 steps in {secs:.1f} s "
-                                       "(OpenMP restatement; meep v1.24 is not available to run)"}
+            "kind": "port", "cpu": cpu_model(), "mpi_ranks": 1,
+            "sample": f"one 96^3 sweep member, {steps} FP64 steps in {secs:.1f} s "
+                      "(OpenMP restatement; meep v1.24 is not available to run)"}
 
 
 def run_reference(args):
@@ -388,6 +411,7 @@ def run_reference(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference", "config": cfg,
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
+                            "cpu": cpu_model(), "mpi_ranks": 1,
                             "sample": f"{per} FP64 steps of one 96^3 sweep member per bench step "
                                       "(CPU restatement; meep v1.24 is not available to run)"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
