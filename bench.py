@@ -37,7 +37,7 @@ METRIC = "voxel-steps/s & %HBM peak: FP32 batched vs FP64 plain at <=1e-4 rel ga
 UNIT = "voxel-steps/s"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=40)
@@ -48,7 +48,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None,
                    help="steps of the end-to-end job (default: the workload's steps per run)")
     p.add_argument("--no-extras", action="store_true", help="skip the FP64 and error legs")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_env():
@@ -56,6 +56,25 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def max_over_ranks(secs, torch):
+    """The slowest rank's time (every rank gets it); identity on one rank.
+    The tensor lives where the process group's backend wants it (NCCL: the
+    GPU, gloo: the host)."""
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(secs)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(secs)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(voxels_per_rank, steps, ws, secs):
+    """Whole-job voxel-steps/s: every rank steps its own batch (weak
+    scaling, replicas), timed by the slowest rank."""
+    return voxels_per_rank * steps * ws / secs
 
 
 def workload_instances(name, rank=0):
@@ -196,11 +215,8 @@ def run_ours(args):
     clocks.start()
     secs, launches = time_steps(f, torch, args.steps, args.warmup)
     clk = clocks.stop()
-    t = torch.tensor([secs], device="cuda")
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    secs = float(t.item())
-    value = voxels * args.steps * ws / secs
+    secs = max_over_ranks(secs, torch)
+    value = job_value(voxels, args.steps, ws, secs)
     peak, peak_kind = measured_peak()
     achieved = bytes_step / (secs / args.steps) / 1e9
     kernel = {"fused": "fused step: plain, slab and multi tile launches per instance group and one general "
