@@ -18,12 +18,14 @@
 //           Two columns per thread where rows are whole (nx % 32 == 0): x-1
 //           H from the neighbouring lane by shuffle, y-1 H recomputed from
 //           L1/L2; otherwise one column per thread recomputing both.
-//   slab    (k_lean_slab): the CPML slabs of one axis; multi (k_lean_multi):
-//           of two or three.  Ten warps per tile: the 8 rows plus one warp
-//           for the row below the tile and one for the column left of it,
-//           which update H only; x-1 H comes by shuffle, y-1 H through a
-//           double-buffered shared plane (one barrier per plane).  Compiled
-//           per axis set, so the other axes' terms vanish.
+//   slab    (k_lean_slab2 / k_lean_slab): the CPML slabs of one axis; multi
+//           (k_lean_multi2 / k_lean_multi): of two or three.  Shared halo:
+//           warps for the row below the tile and the column left of it
+//           update H only; x-1 H comes by shuffle, y-1 H through a
+//           double-buffered shared plane (one barrier per plane).  Two
+//           columns per thread where rows are whole (5 warps per tile: 4
+//           of row pairs, 1 of halo), else one (10 warps: 8 rows, 2 halo).
+//           Compiled per axis set, so the other axes' terms vanish.
 //   general (k_lean_general): an H source in the footprint; also runs the
 //           probe blocks, and its blocks (the only ones that read the step
 //           counter) count themselves: the last advances the step.
@@ -786,6 +788,260 @@ __device__ __forceinline__ void tile_halo(const InstDev<real>& I, int tx, int ty
     }
 }
 
+// ------------------------------------------ two-column shared-halo tiles
+// tile_halo with two columns per thread (instances whose nx is a multiple of
+// 32): a block of LY/2 + 1 warps.  Warps 0..LY/2-1 take the tile's rows as
+// half-warps (row 2w + half; lane l of the half: columns i0+2l, i0+2l+1);
+// the last warp's first half takes the row j0-1 and its second half the
+// column pair (i0-2, i0-1) of rows j0..j0+LY-1 (lane l: row j0+l).  Fields
+// and psi move as pairs; the H at x-1 comes from the neighbouring lane by
+// shuffle (lane 0: from the column half), the H at y-1 through the shared
+// plane, the E at x+2 from the next lane (last lane and column half: loaded).
+// Each element evaluates tile_halo's formulas in the same order, so both
+// bodies give the same bits.
+constexpr int HALO2_THREADS = LX * (LY / 2 + 1);
+
+template <typename real>
+struct HaloIn2 {
+    typename Pair<real>::T ex_n, ey_n, ez, ez_yp, ex_yp, hx, hy, hz;
+    typename Pair<real>::T qy0, qy1, qz0, qz1, qx0, qx1;  // H-side psi (as in HaloIn)
+    real ez_x2, ey_x2;                                    // E at column i+2 of plane k
+};
+template <typename real>
+__device__ __forceinline__ typename Pair<real>::T ld2p(bool on, const real* p, unsigned o) {
+    typename Pair<real>::T v;
+    if (on) return ld2(p, o);
+    v.x = v.y = real(0);
+    return v;
+}
+
+template <typename real, int ZB, int MASK, bool EDGE>
+__device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
+                                               HaloPlane<real>* sh, unsigned qf) {
+    using V2 = typename Pair<real>::T;
+    constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
+    constexpr int NW = LY / 2;  // warps of tile rows
+    const int w = threadIdx.y, l = threadIdx.x & 15, half = threadIdx.x >> 4;
+    const bool own = w < NW, rowh = w == NW && half == 0, colh = w == NW && half == 1;
+    const int r = 2 * w + half;  // own: tile row
+    const int nx = I.nx, ny = I.ny, nz = I.nz;
+    const int i0 = tx * LX, j0 = ty * LY;
+    const int z0 = tz * ZB, z1 = min(nz, z0 + ZB);
+    int i = colh ? i0 - 2 : i0 + 2 * l;
+    int j = own ? j0 + r : (rowh ? j0 - 1 : j0 + min(l, LY - 1));
+    // a cell pair of the grid whose results are used (nx even: i < nx implies i + 1 < nx)
+    const bool act = (!EDGE || (i >= 0 && j >= 0 && i < nx && j < ny)) && (!colh || l < LY);
+    if (EDGE) i = imin(imax(i, 0), nx - 2), j = imin(imax(j, 0), ny - 1);
+
+    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
+    const real* eX = I.F[0][0];
+    const real* eY = I.F[0][1];
+    const real* eZ = I.F[0][2];
+    const real* hX = I.F[0][3];
+    const real* hY = I.F[0][4];
+    const real* hZ = I.F[0][5];
+    real* oEX = I.F[1][0];
+    real* oEY = I.F[1][1];
+    real* oEZ = I.F[1][2];
+    real* oHX = I.F[1][3];
+    real* oHY = I.F[1][4];
+    real* oHZ = I.F[1][5];
+    const real* hiX = SX ? I.psiH[0][0] : nullptr;
+    const real* hiY = SY ? I.psiH[0][1] : nullptr;
+    const real* hiZ = SZ ? I.psiH[0][2] : nullptr;
+    real* hoX = SX ? I.psiH[1][0] : nullptr;
+    real* hoY = SY ? I.psiH[1][1] : nullptr;
+    real* hoZ = SZ ? I.psiH[1][2] : nullptr;
+    real* peX = SX ? I.psiE[0] : nullptr;
+    real* peY = SY ? I.psiE[1] : nullptr;
+    real* peZ = SZ ? I.psiE[2] : nullptr;
+    const real S = I.S;
+
+    const bool yp = !EDGE || j + 1 < ny;
+    const bool xl = l == 15 || colh;             // loads the E of column i+2 itself
+    const bool xp2 = xl && (!EDGE || i + 2 < nx);
+    const bool xm = !EDGE || i0 > 0, ym = !EDGE || j0 > 0;
+    const bool xo0 = SX && in_slab(I, 0, i), xo1 = SX && in_slab(I, 0, i + 1), xo = xo0 || xo1;
+    const bool yo = SY && in_slab(I, 1, j);
+    real bxi0 = 1, cxi0 = 0, bxh0 = 1, cxh0 = 0, bxi1 = 1, cxi1 = 0, bxh1 = 1, cxh1 = 0;
+    real byi = 1, cyi = 0, byh = 1, cyh = 0;
+    if (SX) {
+        const real* pr = I.prof[0];
+        if (xo0) bxi0 = ldg(pr, i), cxi0 = ldg(pr, nx + i), bxh0 = ldg(pr, 2 * nx + i), cxh0 = ldg(pr, 3 * nx + i);
+        if (xo1)
+            bxi1 = ldg(pr, i + 1), cxi1 = ldg(pr, nx + i + 1), bxh1 = ldg(pr, 2 * nx + i + 1),
+            cxh1 = ldg(pr, 3 * nx + i + 1);
+    }
+    if (SY && yo) {
+        const real* pr = I.prof[1];
+        byi = ldg(pr, j), cyi = ldg(pr, ny + j), byh = ldg(pr, 2 * ny + j), cyh = ldg(pr, 3 * ny + j);
+    }
+
+    int k = z0 > 0 ? z0 - 1 : 0;
+    const int k0 = k;
+    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i + qf;  // group member blockIdx.y
+    V2 ex_c = ld2(eX, o), ey_c = ld2(eY, o);
+    V2 hxp, hyp;
+    hxp.x = hxp.y = hyp.x = hyp.y = real(0);
+    const bool xt = SX && (imax(i0 - 1, 0) < I.pl[0] || imin(i0 + LX, nx) - 1 >= nx - I.ph[0]);
+    const unsigned orow = (unsigned)k * plane + (unsigned)j * px + (unsigned)i0 + qf;
+    // a half-warp's 16 lanes take rows 0-15: the z psi rows (SZ) go without
+    volatile unsigned long long* lr =
+        lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, l, xt, yo, qf));
+    for (; k < z1; ++k, o += plane) {
+        const bool kp = !EDGE || k + 1 < nz;
+        const bool store = k >= z0;  // block-uniform
+        const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
+        if (LEAN_PF > 0) {
+            const int kq = k + 1 + LEAN_PF;
+            prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, kq < nz && k + LEAN_PF < z1,
+                                    SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
+        }
+        real bzi = 1, czi = 0, bzh = 1, czh = 0;
+        if (SZ) {
+            const real* pr = I.prof[2];
+            bzi = zo ? ldg(pr, k) : real(1), czi = zo ? ldg(pr, nz + k) : real(0);
+            bzh = zo ? ldg(pr, 2 * nz + k) : real(1), czh = zo ? ldg(pr, 3 * nz + k) : real(0);
+        }
+        const unsigned op = o + qf;
+        // every load of the H update issued together
+        HaloIn2<real> c;
+        c.ex_n = ld2p(kp, eX, o + plane), c.ey_n = ld2p(kp, eY, o + plane);
+        c.ez = ld2(eZ, o);
+        c.ez_yp = ld2p(yp, eZ, o + px), c.ex_yp = ld2p(yp, eX, o + px);
+        c.hx = ld2(hX, o), c.hy = ld2(hY, o), c.hz = ld2(hZ, o);
+        c.qy0 = ld2p(SY && yo, hiY, op), c.qy1 = ld2p(SY && yo, hiY, op + vol);
+        c.qz0 = ld2p(SZ && zo, hiZ, op), c.qz1 = ld2p(SZ && zo, hiZ, op + vol);
+        c.qx0 = ld2p(SX && xo, hiX, op), c.qx1 = ld2p(SX && xo, hiX, op + vol);
+        const real ez_x2l = xp2 ? ldg(eZ, o + 2) : real(0), ey_x2l = xp2 ? ldg(eY, o + 2) : real(0);
+        {
+            const real a = __shfl_down_sync(FULL, c.ez.x, 1, 16), b = __shfl_down_sync(FULL, ey_c.x, 1, 16);
+            c.ez_x2 = xl ? ez_x2l : a;
+            c.ey_x2 = xl ? ey_x2l : b;
+        }
+        const bool sp = store && !dry && own && act;
+
+        // H^{n+1/2} at the thread's two cells
+        V2 hx, hy, hz;
+        {
+            real d1 = c.ez_yp.x - c.ez.x, d2 = c.ey_n.x - ey_c.x, cv = d1 - d2;
+            pml_term_v<SY, true>(cv, yo, byh, cyh, d1, c.qy0.x, hoY, op, sp);
+            pml_term_v<SZ, false>(cv, zo, bzh, czh, d2, c.qz0.x, hoZ, op, sp);
+            hx.x = fma(-S, cv, c.hx.x);
+            d1 = c.ez_yp.y - c.ez.y, d2 = c.ey_n.y - ey_c.y, cv = d1 - d2;
+            pml_term_v<SY, true>(cv, yo, byh, cyh, d1, c.qy0.y, hoY, op + 1, sp);
+            pml_term_v<SZ, false>(cv, zo, bzh, czh, d2, c.qz0.y, hoZ, op + 1, sp);
+            hx.y = fma(-S, cv, c.hx.y);
+        }
+        {
+            real d1 = c.ex_n.x - ex_c.x, d2 = c.ez.y - c.ez.x, cv = d1 - d2;
+            pml_term_v<SZ, true>(cv, zo, bzh, czh, d1, c.qz1.x, hoZ + vol, op, sp);
+            pml_term_v<SX, false>(cv, xo0, bxh0, cxh0, d2, c.qx0.x, hoX, op, sp);
+            hy.x = fma(-S, cv, c.hy.x);
+            d1 = c.ex_n.y - ex_c.y, d2 = c.ez_x2 - c.ez.y, cv = d1 - d2;
+            pml_term_v<SZ, true>(cv, zo, bzh, czh, d1, c.qz1.y, hoZ + vol, op + 1, sp);
+            pml_term_v<SX, false>(cv, xo1, bxh1, cxh1, d2, c.qx0.y, hoX, op + 1, sp);
+            hy.y = fma(-S, cv, c.hy.y);
+        }
+        {
+            real d1 = ey_c.y - ey_c.x, d2 = c.ex_yp.x - ex_c.x, cv = d1 - d2;
+            pml_term_v<SX, true>(cv, xo0, bxh0, cxh0, d1, c.qx1.x, hoX + vol, op, sp);
+            pml_term_v<SY, false>(cv, yo, byh, cyh, d2, c.qy1.x, hoY + vol, op, sp);
+            hz.x = fma(-S, cv, c.hz.x);
+            d1 = c.ey_x2 - ey_c.y, d2 = c.ex_yp.y - ex_c.y, cv = d1 - d2;
+            pml_term_v<SX, true>(cv, xo1, bxh1, cxh1, d1, c.qx1.y, hoX + vol, op + 1, sp);
+            pml_term_v<SY, false>(cv, yo, byh, cyh, d2, c.qy1.y, hoY + vol, op + 1, sp);
+            hz.y = fma(-S, cv, c.hz.y);
+        }
+        if (store) {
+            // the E update's loads ahead of the barrier: S eps_inf^-1 of both
+            // combos and the old E-side psi (the combo loads are unconditional:
+            // every thread's offset is a cell pair of the grid)
+            const bool eo = own && act;
+            const uchar2 cb = __ldg(reinterpret_cast<const uchar2*>(I.combo + o));
+            const real* s0 = I.coef + (int)cb.x * I.ncoef + I.ncoef - 3;
+            const real* s1 = I.coef + (int)cb.y * I.ncoef + I.ncoef - 3;
+            const real a0 = ldg(s0, 0), a1 = ldg(s0, 1), a2 = ldg(s0, 2);
+            const real b0 = ldg(s1, 0), b1 = ldg(s1, 1), b2 = ldg(s1, 2);
+            const V2 pY0 = ld2p(SY && eo && yo, peY, op), pY1 = ld2p(SY && eo && yo, peY, op + vol);
+            const V2 pZ0 = ld2p(SZ && eo && zo, peZ, op), pZ1 = ld2p(SZ && eo && zo, peZ, op + vol);
+            const V2 pX0 = ld2p(SX && eo && xo, peX, op), pX1 = ld2p(SX && eo && xo, peX, op + vol);
+            HaloPlane<real>& b = sh[k & 1];
+            if ((own && r < LY - 1) || rowh) {
+                const int row = rowh ? 0 : r + 1;
+                b.hx[row][2 * l] = hx.x, b.hx[row][2 * l + 1] = hx.y;
+                b.hz[row][2 * l] = hz.x, b.hz[row][2 * l + 1] = hz.y;
+            }
+            if (colh && l < LY) {
+                b.xy[l] = hy.y;
+                b.xz[l] = hz.y;
+            }
+            __syncthreads();
+            if (own) {
+                real hy_m = __shfl_up_sync(FULL, hy.y, 1, 16), hz_m = __shfl_up_sync(FULL, hz.y, 1, 16);
+                if (l == 0) hy_m = xm ? b.xy[r] : real(0), hz_m = xm ? b.xz[r] : real(0);
+                const bool yn = ym || r > 0;
+                V2 hx_ym, hz_ym;
+                hx_ym.x = yn ? b.hx[r][2 * l] : real(0), hx_ym.y = yn ? b.hx[r][2 * l + 1] : real(0);
+                hz_ym.x = yn ? b.hz[r][2 * l] : real(0), hz_ym.y = yn ? b.hz[r][2 * l + 1] : real(0);
+                if (!EDGE || act) {
+                    st2(oHX, o, hx.x, hx.y);
+                    st2(oHY, o, hy.x, hy.y);
+                    st2(oHZ, o, hz.x, hz.y);
+                    const bool si = !dry;
+                    V2 ex, ey, ezn;
+                    {
+                        real d1 = hz.x - hz_ym.x, d2 = hy.x - hyp.x, cv = d1 - d2;
+                        pml_term_v<SY, true>(cv, yo, byi, cyi, d1, pY0.x, peY, op, si);
+                        pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, pZ0.x, peZ, op, si);
+                        ex.x = e_new_v(a0, ex_c.x, cv);
+                        d1 = hz.y - hz_ym.y, d2 = hy.y - hyp.y, cv = d1 - d2;
+                        pml_term_v<SY, true>(cv, yo, byi, cyi, d1, pY0.y, peY, op + 1, si);
+                        pml_term_v<SZ, false>(cv, zo, bzi, czi, d2, pZ0.y, peZ, op + 1, si);
+                        ex.y = e_new_v(b0, ex_c.y, cv);
+                    }
+                    {
+                        real d1 = hx.x - hxp.x, d2 = hz.x - hz_m, cv = d1 - d2;
+                        pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, pZ1.x, peZ + vol, op, si);
+                        pml_term_v<SX, false>(cv, xo0, bxi0, cxi0, d2, pX0.x, peX, op, si);
+                        ey.x = e_new_v(a1, ey_c.x, cv);
+                        d1 = hx.y - hxp.y, d2 = hz.y - hz.x, cv = d1 - d2;
+                        pml_term_v<SZ, true>(cv, zo, bzi, czi, d1, pZ1.y, peZ + vol, op + 1, si);
+                        pml_term_v<SX, false>(cv, xo1, bxi1, cxi1, d2, pX0.y, peX, op + 1, si);
+                        ey.y = e_new_v(b1, ey_c.y, cv);
+                    }
+                    {
+                        real d1 = hy.x - hy_m, d2 = hx.x - hx_ym.x, cv = d1 - d2;
+                        pml_term_v<SX, true>(cv, xo0, bxi0, cxi0, d1, pX1.x, peX + vol, op, si);
+                        pml_term_v<SY, false>(cv, yo, byi, cyi, d2, pY1.x, peY + vol, op, si);
+                        ezn.x = e_new_v(a2, c.ez.x, cv);
+                        d1 = hy.y - hy.x, d2 = hx.y - hx_ym.y, cv = d1 - d2;
+                        pml_term_v<SX, true>(cv, xo1, bxi1, cxi1, d1, pX1.y, peX + vol, op + 1, si);
+                        pml_term_v<SY, false>(cv, yo, byi, cyi, d2, pY1.y, peY + vol, op + 1, si);
+                        ezn.y = e_new_v(b2, c.ez.y, cv);
+                    }
+                    st2(oEX, o, ex.x, ex.y);
+                    st2(oEY, o, ey.x, ey.y);
+                    st2(oEZ, o, ezn.x, ezn.y);
+                }
+            }
+        }
+        hxp = hx;
+        hyp = hy;
+        ex_c = c.ex_n;
+        ey_c = c.ey_n;
+    }
+}
+
+template <typename real, int ZB, int MASK>
+__device__ __forceinline__ void tile_pair_halo_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
+                                                   HaloPlane<real>* sh, unsigned qf) {
+    if (tile_edge(I, tx, ty, tz, ZB))
+        tile_pair_halo<real, ZB, MASK, true>(I, tx, ty, tz, dry, sh, qf);
+    else
+        tile_pair_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh, qf);
+}
+
 template <typename real>
 __device__ __forceinline__ typename Pair<real>::T ld2z(const real* p, unsigned o, bool ok) {
     typename Pair<real>::T v;
@@ -1176,6 +1432,52 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
         tile_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
 }
 
+// Single- and multi-slab tiles with two columns per thread (instances whose
+// nx is a multiple of 32), 5 warps per tile.  (The multi-slab body spills a
+// little at 5 blocks per SM and still runs faster than at 4.)
+#ifndef SJ_LEAN_SLAB2_MINB
+#define SJ_LEAN_SLAB2_MINB 5
+#endif
+#ifndef SJ_LEAN_MULTI2_MINB
+#define SJ_LEAN_MULTI2_MINB 5
+#endif
+template <typename real>
+constexpr int slab2_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB2_MINB : 2; }
+template <typename real>
+constexpr int multi2_minb() { return sizeof(real) == 4 ? SJ_LEAN_MULTI2_MINB : 2; }
+
+template <typename real, int ZB>
+__global__ void __launch_bounds__(HALO2_THREADS, slab2_minb<real>())
+k_lean_slab2(const __grid_constant__ LeanTable<real> tab) {
+    __shared__ HaloPlane<real> sh[2];
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    const unsigned qf = blockIdx.y * tab.qvol;
+    if (m == 1)
+        tile_pair_halo_any<real, ZB, 1>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+    else if (m == 2)
+        tile_pair_halo_any<real, ZB, 2>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+    else
+        tile_pair_halo_any<real, ZB, 4>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+}
+
+template <typename real, int ZB>
+__global__ void __launch_bounds__(HALO2_THREADS, multi2_minb<real>())
+k_lean_multi2(const __grid_constant__ LeanTable<real> tab) {
+    __shared__ HaloPlane<real> sh[2];
+    int tx, ty, tz, m;
+    tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
+    const unsigned qf = blockIdx.y * tab.qvol;
+    if (m == 3)
+        tile_pair_halo_any<real, ZB, 3>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+    else if (m == 5)
+        tile_pair_halo_any<real, ZB, 5>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+    else if (m == 6)
+        tile_pair_halo_any<real, ZB, 6>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+    else
+        tile_pair_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
+}
+
 // Plain tiles with two columns per thread (instances whose nx is a multiple
 // of 32), 4 warps per tile.  (The CPML tile classes keep one column per
 // thread: their two-column bodies need too many registers for the occupancy
@@ -1392,7 +1694,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     const long long gb = general_blocks(gen, dry);
     long long gtotal = gb;
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
-    const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS);
+    const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS), halo2(LX, LY / 2 + 1);
     // descriptor of instance q with the step's parity applied
     auto table = [&](int q) {
         LeanTable<real> t;
@@ -1415,14 +1717,21 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         const LeanTiles& T = tiles[groups[g].lead];
         const unsigned gn = (unsigned)groups[g].n;
         const bool pairs = t.inst.nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
+        const bool pairs2 = pairs;  // CPML tiles too
         cudaStream_t sc[LEAN_CLASSES];
         set_streams(g, sc);
 #define SJ_ZB(Z)                                                                                             \
     case Z:                                                                                                  \
         t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
-        if (t.n_tiles) k_lean_multi<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_MULTI]>>>(t); \
+        if (t.n_tiles && pairs2)                                                                             \
+            k_lean_multi2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_MULTI]>>>(t);          \
+        if (t.n_tiles && !pairs2)                                                                            \
+            k_lean_multi<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_MULTI]>>>(t);            \
         t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
-        if (t.n_tiles) k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);   \
+        if (t.n_tiles && pairs2)                                                                             \
+            k_lean_slab2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_SLAB]>>>(t);            \
+        if (t.n_tiles && !pairs2)                                                                            \
+            k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);              \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
         if (t.n_tiles && pairs)                                                                              \
             k_lean_plain2<real, Z><<<dim3((unsigned)t.n_tiles, gn), half, 0, sc[LEAN_PLAIN]>>>(t);           \
