@@ -23,8 +23,9 @@
 //           warps for the row below the tile and the column left of it
 //           update H only; x-1 H comes by shuffle, y-1 H through a
 //           double-buffered shared plane (one barrier per plane).  Two
-//           columns per thread where rows are whole (5 warps per tile: 4
-//           of row pairs, 1 of halo), else one (10 warps: 8 rows, 2 halo).
+//           columns per thread in FP32 where rows are whole (5 warps per
+//           tile: 4 of row pairs, 1 of halo), else one (10 warps: 8 rows,
+//           2 halo).
 //           Compiled per axis set, so the other axes' terms vanish.
 //   general (k_lean_general): an H source in the footprint; also runs the
 //           probe blocks, and its blocks (the only ones that read the step
@@ -1717,7 +1718,9 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         const LeanTiles& T = tiles[groups[g].lead];
         const unsigned gn = (unsigned)groups[g].n;
         const bool pairs = t.inst.nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
-        const bool pairs2 = pairs;  // CPML tiles too
+        // CPML tiles too in FP32; FP64 keeps one column per thread (its
+        // two-column bodies need 152-168 registers: 2 blocks per SM, slower)
+        const bool pairs2 = pairs && sizeof(real) == 4;
         cudaStream_t sc[LEAN_CLASSES];
         set_streams(g, sc);
 #define SJ_ZB(Z)                                                                                             \
