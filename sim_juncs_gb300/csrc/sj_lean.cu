@@ -1726,13 +1726,15 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 #define SJ_ZB(Z)                                                                                             \
     case Z:                                                                                                  \
         t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
-        if (t.n_tiles && pairs2)                                                                             \
-            k_lean_multi2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_MULTI]>>>(t);          \
+        if constexpr (sizeof(real) == 4)                                                                     \
+            if (t.n_tiles && pairs2)                                                                         \
+                k_lean_multi2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_MULTI]>>>(t);      \
         if (t.n_tiles && !pairs2)                                                                            \
             k_lean_multi<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_MULTI]>>>(t);            \
         t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
-        if (t.n_tiles && pairs2)                                                                             \
-            k_lean_slab2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_SLAB]>>>(t);            \
+        if constexpr (sizeof(real) == 4)                                                                     \
+            if (t.n_tiles && pairs2)                                                                         \
+                k_lean_slab2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_SLAB]>>>(t);        \
         if (t.n_tiles && !pairs2)                                                                            \
             k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);              \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
