@@ -148,26 +148,30 @@ __host__ __device__ inline bool tile_edge(const InstDev<real>& I, int tx, int ty
 
 // The rows a column march prefetches into L2, LEAN_PF planes ahead, spread
 // one row per lane (a single predicated instruction per warp and plane):
-// lanes 0-5 the six field components, 6 the combo bytes, 7-10 the two psi
-// slots of H and of E along x (tiles touching an x slab), 11-14 those along
-// y (rows in a y slab), 15-18 those along z (planes in a z slab).  A lane's
-// row is one word: the array's address (16-byte aligned) with bit 0 set for
-// a z psi row and bit 1 for a byte array; 0 = no row.  The word waits in a
-// shared-memory slot of the thread and is reloaded on every plane, so it
-// holds no register across the march.  The element offset a row is
-// prefetched at is a field offset; psi rows add qf (a group member's psi
-// sits twice as far from the lead's as its fields).
+// lanes 0-5 the six field components, 6 the combo bytes, then four rows per
+// CPML axis the tile's row uses (the two psi slots of H and of E), axes in
+// x, y, z order and packed: x when the tile touches an x slab, y when the
+// row is in a y slab, z (only on planes in a z slab) in any tile with SZ.
+// At most 19 rows, so a 16-lane half-warp covers every single- and
+// two-axis tile.  A lane's row is one word: the array's address (16-byte
+// aligned) with bit 0 set for a z psi row and bit 1 for a byte array; 0 =
+// no row.  The word waits in a shared-memory slot of the thread and is
+// reloaded on every plane, so it holds no register across the march.  The
+// element offset a row is prefetched at is a field offset; psi rows add qf
+// (a group member's psi sits twice as far from the lead's as its fields).
 template <typename real, bool SX, bool SY, bool SZ>
 __device__ __forceinline__ unsigned long long lane_row(const InstDev<real>& I, int l, bool xt, bool yt,
                                                        unsigned qf = 0) {
     if (l < 6) return (unsigned long long)I.F[0][l];
     if (l == 6) return (unsigned long long)I.combo | 2ull;
-    if (l < 19) {
-        const int a = (l - 7) >> 2, q = (l - 7) & 3;
-        if (a == 0 ? SX && xt : (a == 1 ? SY && yt : SZ)) {
-            const real* b = q < 2 ? I.psiH[0][a] : I.psiE[a];
-            return (unsigned long long)(b + qf + ((q & 1) ? I.vol : 0)) | (a == 2 ? 1ull : 0ull);
+    int m = l - 7;  // index among the psi rows in use
+    for (int a = 0; a < 3; ++a) {
+        if (!(a == 0 ? SX && xt : (a == 1 ? SY && yt : SZ))) continue;
+        if (m < 4) {
+            const real* b = m < 2 ? I.psiH[0][a] : I.psiE[a];
+            return (unsigned long long)(b + qf + ((m & 1) ? I.vol : 0)) | (a == 2 ? 1ull : 0ull);
         }
+        m -= 4;
     }
     return 0;
 }
@@ -886,7 +890,7 @@ __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, i
     hxp.x = hxp.y = hyp.x = hyp.y = real(0);
     const bool xt = SX && (imax(i0 - 1, 0) < I.pl[0] || imin(i0 + LX, nx) - 1 >= nx - I.ph[0]);
     const unsigned orow = (unsigned)k * plane + (unsigned)j * px + (unsigned)i0 + qf;
-    // a half-warp's 16 lanes take rows 0-15: the z psi rows (SZ) go without
+    // a half-warp's 16 lanes take rows 0-15 (three-axis tiles: the z psi rows go without)
     volatile unsigned long long* lr =
         lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, l, xt, yo, qf));
     for (; k < z1; ++k, o += plane) {
@@ -1132,7 +1136,7 @@ __device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty
     const int k0 = k;
     const int i0 = tx * LX;
     const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
-    // a half-warp's 16 lanes take rows 0-15: the z psi rows (SZ) go without
+    // a half-warp's 16 lanes take rows 0-15 (three-axis tiles: the z psi rows go without)
     volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, lane, xt, yo, qf));
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < nz;
