@@ -268,6 +268,11 @@ int sj_synchronize(sj_sim* sim);
    zseg planes.  Applies to the schedule selected when it is called. */
 int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg);
 int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* ring, int32_t* zseg);
+/* FUSED: columns per thread in the tile kernels.  0 (default) = two where
+   rows are whole (nx a multiple of 32; CPML tiles in FP32 only), 1 = one
+   everywhere.  Both evaluate the same per-cell arithmetic in the same order:
+   the results do not change. */
+int sj_set_fused_columns(sj_sim* sim, int32_t columns);
 /* time every fused tiling with `steps` launches that leave the state
    untouched, keep the fastest and report it (any output may be NULL) */
 int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* ring, int32_t* zseg,

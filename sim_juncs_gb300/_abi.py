@@ -140,6 +140,7 @@ SIGNATURES = {
     "sj_read_dft": (C.c_int, [_P, C.c_int32, _D, C.c_size_t]),
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),
     "sj_set_snapshots": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "sj_set_fused_columns": (C.c_int, [_P, C.c_int32]),
     "sj_take_snapshot": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64), _D, C.c_size_t]),
     "sj_snapshots_pending": (C.c_int32, [_P, C.c_int32]),
     "sj_write_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

@@ -162,6 +162,7 @@ struct sj_sim {
     // fused (lean) schedule: z-segment length (descriptors travel as kernel
     // parameters) and the side streams its kernels overlap on
     int l_zb = 16;
+    int l_one_column = 0;              // 1: one column per thread in every tile kernel
     int lean_zb = -1;                  // z-segment length the tile lists were built for
     void* d_tiles = nullptr;           // tile lists of all instances and classes
     std::vector<LeanTiles> ltiles;     // per instance
@@ -927,7 +928,7 @@ cudaError_t launch_one(sj_sim* sim) {
         prepare_lean<real>(sim);
         e = launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), sim->ltiles.data(), sim->lgroups.data(),
                                    (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur,
-                                   sim->d_state, lean_streams(sim));
+                                   sim->d_state, lean_streams(sim), sim->l_one_column);
     } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
@@ -959,13 +960,13 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
         const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
         ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
                                   (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
-                                  sim->d_state, ls),
+                                  sim->d_state, ls, sim->l_one_column),
            "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
             ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
                                       (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
-                                      sim->d_state, ls),
+                                      sim->d_state, ls, sim->l_one_column),
                "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
@@ -1677,6 +1678,14 @@ int sj_set_tiling(sj_sim* sim, int32_t tile_y, int32_t ring, int32_t zseg) {
     sim->f_ring = ring;
     sim->f_zs = zseg;
     sim->fused_ready = false;
+    sim->drop_graphs();
+    return SJ_OK;
+}
+
+int sj_set_fused_columns(sj_sim* sim, int32_t columns) {
+    if (!sim) return SJ_E_INVALID;
+    if (columns != 0 && columns != 1) return finish(sim, SJ_E_INVALID, "columns must be 0 (automatic) or 1");
+    sim->l_one_column = columns;
     sim->drop_graphs();
     return SJ_OK;
 }

@@ -187,7 +187,7 @@ template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
                              const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
                              int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls);
+                             int cur, DevState* st, const LeanStreams& ls, int one_column = 0);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>

@@ -1686,7 +1686,7 @@ template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
                              const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
                              int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls) {
+                             int cur, DevState* st, const LeanStreams& ls, int one_column) {
     cudaError_t e = cudaSuccess;
     const bool fork = ls.side[0] != nullptr;
     const int nsets = fork ? std::min(std::max(n_groups, 1), LEAN_SETS) : 0;
@@ -1721,7 +1721,8 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         LeanTable<real> t = table(groups[g].lead);
         const LeanTiles& T = tiles[groups[g].lead];
         const unsigned gn = (unsigned)groups[g].n;
-        const bool pairs = t.inst.nx % LX == 0;  // plain tiles: two columns per thread where rows are whole
+        // plain tiles: two columns per thread where rows are whole
+        const bool pairs = !one_column && t.inst.nx % LX == 0;
         // CPML tiles too in FP32; FP64 keeps one column per thread (its
         // two-column bodies need 152-168 registers: 2 blocks per SM, slower)
         const bool pairs2 = pairs && sizeof(real) == 4;
@@ -1796,8 +1797,9 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*,
                                               const InstDev<double>*, const LeanTiles*, const LeanGroup*, int,
                                               const LeanGen&, const LeanFix&, int, int, int, int, DevState*,
-                                              const LeanStreams&);
+                                              const LeanStreams&, int);
 template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const InstDev<float>*,
                                              const LeanTiles*, const LeanGroup*, int, const LeanGen&,
-                                             const LeanFix&, int, int, int, int, DevState*, const LeanStreams&);
+                                             const LeanFix&, int, int, int, int, DevState*, const LeanStreams&,
+                                             int);
 }  // namespace sj

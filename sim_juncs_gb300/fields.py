@@ -78,6 +78,11 @@ class Fields:
         32 x tile_y tiles, TMA ring depth, z segments)."""
         self._ck(self.lib.sj_set_tiling(self.handle, int(tile_y), int(ring), int(zseg)))
 
+    def set_fused_columns(self, columns):
+        """Fused schedule: 0 = two columns per thread where rows are whole
+        (default), 1 = one column per thread everywhere (same results)."""
+        self._ck(self.lib.sj_set_fused_columns(self.handle, int(columns)))
+
     def tiling(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         self._ck(self.lib.sj_get_tiling(self.handle, C.byref(a), C.byref(b), C.byref(c)))

@@ -174,6 +174,24 @@ def test_fused_zsegments_agree(lib, zs):
     np.testing.assert_array_equal(b.monitors(), a.monitors())
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_two_column_tiles_equal_one_column(lib, precision):
+    # nx = 96: plain, single-slab and multi-slab tiles all run two columns
+    # per thread by default (CPML tiles in FP32); forcing one column per
+    # thread must not change a bit
+    inst = junction_instance(n=96, res=30.0, probe_components=("Ex", "Ez"))
+    assert plain_tiles(inst, 16) > 0
+    a = Fields(inst, precision, "fused")
+    b = Fields(inst, precision, "fused")
+    b.set_fused_columns(1)
+    a.step(80)
+    b.step(80)
+    for c in range(6):
+        np.testing.assert_array_equal(a.get_array(c), b.get_array(c), err_msg=f"component {c}")
+    np.testing.assert_array_equal(a.monitors(), b.monitors())
+    np.testing.assert_array_equal(a.dft(), b.dft())
+
+
 def plain_tiles(inst, zb):
     """A lower bound on the tiles the fused schedule gives its plain kernel
     (32 x 8 x zb tiles whose footprint, one cell wider towards -x/-y/-z,
