@@ -850,16 +850,30 @@ void prepare_lean(sj_sim* sim) {
         }
         general[q] = lists[LEAN_GENERAL];
     }
-    // a group's launches use the lead's lists: its members' must be equal
-    for (const auto& mem : sim->lmembers)
-        for (size_t r = 1; r < mem.size(); ++r)
-            for (int c = 0; c < LEAN_CLASSES; ++c) {
-                const long long n = sim->ltiles[mem[0]].count[c];
-                const unsigned* a = all.data() + off[(size_t)mem[0] * LEAN_CLASSES + c];
-                const unsigned* b = all.data() + off[(size_t)mem[r] * LEAN_CLASSES + c];
-                if (sim->ltiles[mem[r]].count[c] != n || (n && memcmp(a, b, n * sizeof(unsigned)) != 0))
-                    fail(SJ_E_INVALID, "internal: members of a launch group have different tile lists");
+    // Launch groups: a group's launches use its lead's plain, slab and multi
+    // lists, so a packed group splits into runs of consecutive members whose
+    // lists are equal (a design region turns tiles general in one member
+    // only); a run keeps the fixed stride from its own first member.
+    auto same_lists = [&](int a, int b) {
+        for (int c = 0; c < LEAN_CLASSES; ++c) {
+            if (c == LEAN_GENERAL) continue;
+            const long long n = sim->ltiles[a].count[c];
+            if (sim->ltiles[b].count[c] != n) return false;
+            if (n && memcmp(all.data() + off[(size_t)a * LEAN_CLASSES + c],
+                            all.data() + off[(size_t)b * LEAN_CLASSES + c], n * sizeof(unsigned)) != 0)
+                return false;
+        }
+        return true;
+    };
+    sim->lgroups.clear();
+    for (const auto& mem : sim->lmembers) {
+        size_t first = 0;
+        for (size_t r = 1; r <= mem.size(); ++r)
+            if (r == mem.size() || !same_lists(mem[first], mem[r])) {
+                sim->lgroups.push_back(LeanGroup{mem[first], (int)(r - first)});
+                first = r;
             }
+    }
     sim->dfree(sim->d_tiles);
     sim->d_tiles = sim->upload(all);
     const unsigned* base = reinterpret_cast<const unsigned*>(sim->d_tiles);
@@ -1234,11 +1248,14 @@ void set_design_t(sj_sim* sim, int q, const sj_design_desc* d) {
         H.d_dinv = sim->upload(inv);
         I.dinv = H.d_dinv;
         for (int a = 0; a < 3; ++a) I.des_lo[a] = d->lo[a], I.des_n[a] = d->n[a];
-        // the per-voxel eps is applied by the split schedule's E update
-        sim->schedule = SJ_SCHED_SPLIT;
+        // the per-voxel eps is applied by the split schedule's E update and by
+        // the fused schedule's general tiles; the TMA schedule has neither
+        if (sim->schedule == SJ_SCHED_TMA) sim->schedule = SJ_SCHED_FUSED;
     }
     sim->drop_graphs();
+    sim->lean_zb = -1;  // the design's tiles move to the general class
     upload_table<real>(sim);
+    if (sim->schedule == SJ_SCHED_FUSED) prepare_lean<real>(sim);
 }
 
 template <typename real>
@@ -1276,11 +1293,10 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
     if (backward && total_d > 0 && (!grad || (size_t)total_d > cap))
         fail(SJ_E_RANGE, "d_obj_d_eps too small for the design voxels");
     if (!backward) K = N;  // the final state is the only one kept
-    sim->schedule = SJ_SCHED_SPLIT;
-    sim->drop_graphs();
+    if (sim->schedule == SJ_SCHED_TMA) fail(SJ_E_INVALID, "the adjoint steps with the fused or split schedule");
     ensure_capacity<real>(sim, N);
+    prepare_schedule<real>(sim);
     cudaStream_t st = sim->stream;
-    const int cur = sim->cur;
     std::vector<void*> temps;  // freed at the end
     auto tmp = [&](size_t bytes) {
         void* p = sim->dalloc(bytes);
@@ -1292,29 +1308,37 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
         void* p;
         size_t bytes;
     };
-    std::vector<Arr> state;
-    for (int q = 0; q < ni; ++q) {
-        const InstDev<real>& I = dv[q];
-        const size_t vb = (size_t)I.vol * sizeof(real);
-        for (int c = 0; c < 6; ++c) state.push_back({I.F[cur][c], vb});
-        for (int a = 0; a < 3; ++a)
-            if (I.psiE[a]) state.push_back({I.psiE[a], 2 * vb}), state.push_back({I.psiH[cur][a], 2 * vb});
-        if (I.P) state.push_back({I.P, (size_t)I.n_poles * 6 * I.dvol * sizeof(real)});
-    }
+    // the arrays holding the state while the ping-pong parity is p (the
+    // fused schedule flips it every step; the split one stays in place)
+    auto state_of = [&](int p) {
+        std::vector<Arr> v;
+        for (int q = 0; q < ni; ++q) {
+            const InstDev<real>& I = dv[q];
+            const size_t vb = (size_t)I.vol * sizeof(real);
+            for (int c = 0; c < 6; ++c) v.push_back({I.F[p][c], vb});
+            for (int a = 0; a < 3; ++a)
+                if (I.psiE[a]) v.push_back({I.psiE[a], 2 * vb}), v.push_back({I.psiH[p][a], 2 * vb});
+            if (I.P) v.push_back({I.P, (size_t)I.n_poles * 6 * I.dvol * sizeof(real)});
+        }
+        return v;
+    };
     size_t sbytes = 0;
-    for (const Arr& a : state) sbytes += a.bytes;
+    for (const Arr& a : state_of(0)) sbytes += a.bytes;
     const long long nseg = (N + K - 1) / K;
     char* arena = (char*)tmp((size_t)(nseg + 1) * sbytes);
+    std::vector<int> slot_cur(nseg + 1, 0);  // the parity each checkpoint was taken at
     auto save = [&](long long slot) {
         size_t off = (size_t)slot * sbytes;
-        for (const Arr& a : state) {
+        for (const Arr& a : state_of(sim->cur)) {
             ck(cudaMemcpyAsync(arena + off, a.p, a.bytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
             off += a.bytes;
         }
+        slot_cur[slot] = sim->cur;
     };
     auto restore = [&](long long slot) {
+        sim->cur = slot_cur[slot];
         size_t off = (size_t)slot * sbytes;
-        for (const Arr& a : state) {
+        for (const Arr& a : state_of(sim->cur)) {
             ck(cudaMemcpyAsync(a.p, arena + off, a.bytes, cudaMemcpyDeviceToDevice, st), "restore");
             off += a.bytes;
         }
@@ -1331,7 +1355,7 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
         d_D[q] = (double2*)tmp((size_t)nc * 3 * sizeof(double2));
     }
     // ---- forward from rest, keeping the state every K steps and at the end
-    for (const Arr& a : state) ck(cudaMemsetAsync(a.p, 0, a.bytes, st), "reset");
+    for (const Arr& a : state_of(sim->cur)) ck(cudaMemsetAsync(a.p, 0, a.bytes, st), "reset");
     for (int q = 0; q < ni; ++q)
         if (dv[q].dft) ck(cudaMemsetAsync(dv[q].dft, 0, (size_t)hv[q].n_dft * hv[q].n_freq * sizeof(double2), st), "reset");
     sim->t = 0;
@@ -1339,8 +1363,8 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
     for (long long n = 0; n < N; ++n) {
         if (n % K == 0) save(n / K);
         for (int q = 0; q < ni; ++q)
-            ck(launch_objective<real>(dv[q], cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask, objs[q].frequency,
-                                      d_D[q], n, true, nullptr, st),
+            ck(launch_objective<real>(dv[q], sim->cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask,
+                                      objs[q].frequency, d_D[q], n, true, nullptr, st),
                "objective");
         ck(launch_one<real>(sim), "step launch");
     }
@@ -1406,7 +1430,7 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
             for (int q = 0; q < ni; ++q) {
                 A[q].rec_t0 = t0;
                 ck(launch_adjoint_step<real>(A[q], n, st), "adjoint step");
-                ck(launch_objective<real>(dv[q], cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask,
+                ck(launch_objective<real>(dv[q], sim->cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask,
                                           objs[q].frequency, d_D[q], n, false, A[q].eb, st),
                    "adjoint source");
             }
@@ -1623,8 +1647,8 @@ int sj_set_schedule(sj_sim* sim, int32_t schedule) {
     if (schedule != SJ_SCHED_FUSED && schedule != SJ_SCHED_SPLIT && schedule != SJ_SCHED_TMA)
         return finish(sim, SJ_E_INVALID, "unknown schedule");
     const bool des = sim->precision == SJ_F64 ? any_design<double>(sim) : any_design<float>(sim);
-    if (des && schedule != SJ_SCHED_SPLIT)
-        return finish(sim, SJ_E_INVALID, "instances with a design region step with the split schedule");
+    if (des && schedule == SJ_SCHED_TMA)
+        return finish(sim, SJ_E_INVALID, "instances with a design region step with the fused or split schedule");
     sim->schedule = schedule;
     return SJ_OK;
 }

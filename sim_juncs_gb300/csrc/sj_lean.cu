@@ -139,6 +139,15 @@ __host__ __device__ inline bool tile_has_hsource(const InstDev<real>& I, int i0,
     return false;
 }
 
+// Does the tile own a cell of the design region (adjoint)?  Those cells
+// scale by their own eps^-1, which only the general kernel applies.
+template <typename real>
+__host__ __device__ inline bool tile_has_design(const InstDev<real>& I, int i0, int j0, int z0, int z1) {
+    if (!I.dinv) return false;
+    return i0 < I.des_lo[0] + I.des_n[0] && i0 + LX > I.des_lo[0] && j0 < I.des_lo[1] + I.des_n[1] &&
+           j0 + LY > I.des_lo[1] && z0 < I.des_lo[2] + I.des_n[2] && z1 > I.des_lo[2];
+}
+
 // Does the tile's footprint or its z+1 plane reach a face of the grid?
 template <typename real>
 __host__ __device__ inline bool tile_edge(const InstDev<real>& I, int tx, int ty, int tz, int zb) {
@@ -358,6 +367,42 @@ __device__ __forceinline__ real e_new_v(real sinv, real e_old, real cv) {
     return fma(sinv, cv, e_old);
 }
 
+// Design region (adjoint): the cell's index in the design box, or -1
+template <typename real>
+__device__ __forceinline__ long long design_index(const InstDev<real>& I, int i, int j, int k) {
+    if (!I.dinv) return -1;
+    const int u = i - I.des_lo[0], v = j - I.des_lo[1], w = k - I.des_lo[2];
+    if ((unsigned)u >= (unsigned)I.des_n[0] || (unsigned)v >= (unsigned)I.des_n[1] ||
+        (unsigned)w >= (unsigned)I.des_n[2])
+        return -1;
+    return ((long long)w * I.des_n[1] + v) * I.des_n[0] + u;
+}
+// where the E-update bracket of design cell d, component c, at step n is
+// recorded while a segment is re-run (null: not recording)
+template <typename real>
+__device__ __forceinline__ real* design_rec(const InstDev<real>& I, long long d, long long n, int c) {
+    if (d < 0 || !I.rec_acc || n < I.rec_t0 || n >= I.rec_t0 + I.rec_len) return nullptr;
+    const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
+    return I.rec_acc + ((n - I.rec_t0) * nd + d) * 3 + c;
+}
+// E^{n+1} in a general tile: a design cell scales by S times its own eps^-1
+// and, while recording, keeps the bracket S curl H (the corrections subtract
+// the source and polarisation terms from it: the bracket of
+// E^{n+1} = E^n + eps^-1 (S curl H - dt J - dP))
+template <int CA, bool EXTRAS, typename real>
+__device__ __forceinline__ real e_new_g(const InstDev<real>& I, const real* cf, real e_old, real cv, int i, int j,
+                                        int k, long long n, bool dry) {
+    if (EXTRAS) {
+        const long long d = design_index(I, i, j, k);
+        if (d >= 0) {
+            if (!dry)
+                if (real* r = design_rec(I, d, n, CA)) *r = I.S * cv;
+            return fma(I.S * I.dinv[d], cv, e_old);
+        }
+    }
+    return e_new<CA>(I, cf, e_old, cv);
+}
+
 // Slab axes a tile's footprint touches (bit a = axis a): the same footprint
 // test as the host's plain box.
 template <typename real>
@@ -545,21 +590,21 @@ __device__ __forceinline__ void tile_block(const InstDev<real>& I, int tx, int t
                 real cv = d1 - d2;
                 pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
                 pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
-                oEX[o] = e_new<0>(I, cf, ex_c, cv);
+                oEX[o] = e_new_g<0, EXTRAS>(I, cf, ex_c, cv, i, j, k, n, dry);
             }
             {
                 const real d1 = hx - hxp, d2 = hz - hz_xm;
                 real cv = d1 - d2;
                 pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
                 pml_term<SX, false, false>(cv, xo, bxi, cxi, d2, peX, peX, o, si);
-                oEY[o] = e_new<1>(I, cf, ey_c, cv);
+                oEY[o] = e_new_g<1, EXTRAS>(I, cf, ey_c, cv, i, j, k, n, dry);
             }
             {
                 const real d1 = hy - hy_xm, d2 = hx - hx_ym;
                 real cv = d1 - d2;
                 pml_term<SX, true, false>(cv, xo, bxi, cxi, d1, peX + vol, peX + vol, o, si);
                 pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
-                oEZ[o] = e_new<2>(I, cf, ez, cv);
+                oEZ[o] = e_new_g<2, EXTRAS>(I, cf, ez, cv, i, j, k, n, dry);
             }
         }
         hxp = hx;
@@ -1551,9 +1596,12 @@ k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
         const int di = (int)(cell % sv.n[0]), dj = (int)((cell / sv.n[0]) % sv.n[1]), dk = (int)(cell / n01);
         const long long o = (long long)(sv.lo[2] + dk) * I.plane + (long long)(sv.lo[1] + dj) * I.px + (sv.lo[0] + di);
         real* E = I.F[cur ^ 1][sv.comp];
-        const real cfc = I.coef[(int)I.combo[o] * I.ncoef + sv.comp];
+        const long long d = design_index(I, sv.lo[0] + di, sv.lo[1] + dj, sv.lo[2] + dk);
+        const real cfc = d >= 0 ? I.dinv[d] : I.coef[(int)I.combo[o] * I.ncoef + sv.comp];
         const real J = (real)sv.tab[n] * sv.w[0][di] * sv.w[1][dj] * sv.w[2][dk];
         E[o] = fma(-cfc, J, E[o]);
+        if (!dry)
+            if (real* r = design_rec(I, d, n, sv.comp)) *r -= J;
     }
     finish_block(step_blocks, dry, st);
 }
@@ -1565,6 +1613,7 @@ template <typename real>
 __global__ void __launch_bounds__(FIX_THREADS)
 k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int cur, unsigned step_blocks,
             int dry, DevState* st) {
+    const long long n = st->step;
     const int2 e = __ldg(blk + blockIdx.x);
     const InstDev<real>& I = insts[e.x];
     const long long di = (long long)e.y * FIX_THREADS + threadIdx.x;
@@ -1591,7 +1640,10 @@ k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
                     }
                 }
                 real* E = I.F[cur ^ 1][c];
-                E[o] = fma(-cf[c], corr, E[o]);
+                const long long d = design_index(I, i, j, k);
+                E[o] = fma(-(d >= 0 ? I.dinv[d] : cf[c]), corr, E[o]);
+                if (!dry)
+                    if (real* r = design_rec(I, d, n, c)) *r -= corr;
             }
         }
     }
@@ -1612,7 +1664,7 @@ int lean_classify(const InstDev<real>& I, int zb, std::vector<unsigned>* lists) 
             for (int tx = 0; tx < ntx; ++tx) {
                 const int i0 = tx * LX, j0 = ty * LY, z0 = tz * zb, z1 = imin(I.nz, z0 + zb);
                 const int m = tile_slab_mask(I, i0, j0, z0, z1);
-                const int c = tile_has_hsource(I, i0, j0, z0, z1) ? LEAN_GENERAL
+                const int c = tile_has_hsource(I, i0, j0, z0, z1) || tile_has_design(I, i0, j0, z0, z1) ? LEAN_GENERAL
                               : m == 0                      ? LEAN_PLAIN
                               : (m == 1 || m == 2 || m == 4) ? LEAN_SLAB
                                                              : LEAN_MULTI;

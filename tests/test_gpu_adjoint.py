@@ -98,14 +98,39 @@ def test_batched_designs_equal_separate_runs(lib):
         np.testing.assert_array_equal(gb[q], g1[0])
 
 
-def test_design_region_requires_the_split_schedule(lib):
+def test_design_region_steps_with_fused_or_split(lib):
+    # the fused schedule (default) applies the design eps in its general
+    # tiles, the split one in its E pass; the TMA schedule has no design path
     inst, des, obj = setup()
     f = Fields(inst, "f32")
     f.set_design(des)
-    with pytest.raises(_abi.SJError):
-        f.set_schedule("fused")
-    f.set_design(None)
+    assert f.schedule_name() == "fused"
+    f.set_schedule("split")
     f.set_schedule("fused")
+    with pytest.raises(_abi.SJError):
+        f.set_schedule("tma")
+    f.set_design(None)
+    f.set_schedule("tma")
+    f.set_design(des)                      # a TMA simulation moves to fused
+    assert f.schedule_name() == "fused"
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-10), ("f32", 1e-4)])
+def test_fused_and_split_adjoints_agree(lib, precision, tol):
+    # the same discrete adjoint whichever schedule runs the forward passes:
+    # the two differ only in rounding (fused: explicit FMAs, bracket recorded
+    # in pieces across the tile and correction kernels)
+    inst, des, obj = setup()
+    out = []
+    for sched in ("fused", "split"):
+        f = Fields(inst, precision, sched)
+        f.set_design(des)
+        f.set_schedule(sched)
+        out.append(f.adjoint_gradient(obj, N_STEPS, checkpoint_every=50))
+        f.close()
+    (Fa, ga), (Fb, gb) = out
+    assert Fa[0] == pytest.approx(Fb[0], rel=tol)
+    assert rel(ga[0], gb[0]) <= tol
 
 
 def test_torch_autograd_binding(lib):
