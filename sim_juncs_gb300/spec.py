@@ -34,6 +34,20 @@ class Grid:
         return self.nx * self.ny * self.nz
 
 
+def reference_grid(length, pml_thickness, resolution, grid_num=-1, courant=0.5, origin=(0.0, 0.0, 0.0)):
+    """The reference's grid rounding (correct_defaults, src/argparse.h:171-191)
+    for a cubic cell of side length + 2 pml_thickness: unless grid_num is
+    given, grid_num = 2 int(0.5 (1 + L_tot res)) + 1 (an odd number of
+    points), then res = grid_num / L_tot.  Returns (Grid with dx = 1 / res
+    and dt = courant dx, the rounded resolution)."""
+    total = length + 2 * pml_thickness
+    if grid_num < 0:
+        grid_num = 2 * int(0.5 * (1 + total * resolution)) + 1
+    res = grid_num / total
+    dx = 1.0 / res
+    return Grid(grid_num, grid_num, grid_num, dx, courant * dx, tuple(origin)), res
+
+
 @dataclass
 class Susceptibility:
     """One drude_suscept (src/disp.hpp:88-93) in meep units (already / um_scale)."""

@@ -21,7 +21,7 @@ from oracle import oracle
 from sim_juncs_gb300 import _abi
 from sim_juncs_gb300.configs import gaussian_pulse
 from sim_juncs_gb300.geometry import Program
-from sim_juncs_gb300.spec import Grid, Region, Scene, Source, Susceptibility, scene_to_c
+from sim_juncs_gb300.spec import Grid, Region, Scene, Source, Susceptibility, reference_grid, scene_to_c
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "cgs_reference.json")
 
@@ -171,3 +171,18 @@ def test_spectrum_restatement_matches_reference_fft():
         assert len(got) == c["out_len"], c["n"]
         scale = max(1.0, float(np.max(np.abs(want))))
         assert float(np.max(np.abs(got - want))) <= 1e-12 * scale, c["n"]
+
+
+def test_reference_grid_rounding():
+    # src/main_test.cpp:1658 (tests/test.conf: length 16, pml 2, resolution
+    # 1.5 -> 31 points, 1.55 px/um) and :1703 (--length 9, pml 2,
+    # --grid-res 3 -> 41 points, 3.1538 px/um); the junction cell of 3.2 um
+    # at 20 px/um rounds to 65 points
+    g, res = reference_grid(16.0, 2.0, 1.5)
+    assert (g.nx, res) == (31, 1.55)
+    g, res = reference_grid(9.0, 2.0, 3.0)
+    assert g.nx == 41 and res == pytest.approx(3.1538, abs=5e-5)
+    g, res = reference_grid(2.2, 0.5, 20.0)
+    assert g.nx == 65 and g.dt == pytest.approx(0.5 * g.dx)
+    g, res = reference_grid(2.2, 0.5, 20.0, grid_num=64)   # an explicit grid number is kept
+    assert g.nx == 64 and res == 20.0
