@@ -7,11 +7,14 @@
 // (eps_inf^{-1}, the polarisation ADE, the E-side psi, the backward
 // differences of H), then the transpose of the H update (the H-side psi and
 // the forward differences of E).  A difference's adjoint is scattered to the
-// two cells it reads; each kernel pair writes the per-cell adjoints of both
-// differences (t1, t2) and then gathers them, one thread per cell, so no two
-// threads write one value.  The gradient with respect to a design voxel's
-// inverse eps is sum_n dF/dE^{n+1} * acc^n, acc^n being the E update's
-// bracket at step n, recorded while the segment is re-run forward.
+// two cells it reads: a kernel writes the per-cell adjoints of both
+// differences (t1, t2 for the E update, t3, t4 for the H update) and the
+// next gathers them, one thread per cell, so no two threads write one value.
+// Three passes per step: k_adj_e, k_adj_e_gather_h (the gather into dF/dH
+// and, at the same cell, the H update's transpose), k_adj_h_gather.  The
+// gradient with respect to a design voxel's inverse eps is
+// sum_n dF/dE^{n+1} * acc^n, acc^n being the E update's bracket at step n,
+// recorded while the segment is re-run forward.
 // One launch per instance; the descriptor travels as a kernel parameter.
 #include "sj_physics.cuh"
 
@@ -98,38 +101,32 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDe
     }
 }
 
-// dF/dH^{n+1/2} += what the E update's differences read from H at this cell.
+// dF/dH^{n+1/2} += what the E update's differences read from H at this cell
+// (t1, t2 of this cell and its +1 neighbours); then, at the same cell, the
+// transpose of the H update: hb carries over unchanged to H^{n-1/2}, its
+// share through the curl of E goes to t3, t4.
 template <typename real>
-__global__ void __launch_bounds__(AX * AY) k_adj_e_gather(const __grid_constant__ AdjDev<real> A) {
+__global__ void __launch_bounds__(AX * AY) k_adj_e_gather_h(const __grid_constant__ AdjDev<real> A) {
     const InstDev<real>& I = A.I;
     const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
     if (i >= I.nx || j >= I.ny) return;
     const long long o = (long long)k * I.plane + (long long)j * I.px + i;
     const int idx[3] = {i, j, k};
+    real hb[3] = {A.hb[0][o], A.hb[1][o], A.hb[2][o]};
     for (int ca = 0; ca < 3; ++ca) {
         const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
         real v = A.t1[ca][o];
         if (idx[a1] + 1 < dim_of(I, a1)) v -= A.t1[ca][o + stride_of(I, a1)];
-        A.hb[a2][o] += v;
+        hb[a2] += v;
         real w = A.t2[ca][o];
         if (idx[a2] + 1 < dim_of(I, a2)) w -= A.t2[ca][o + stride_of(I, a2)];
-        A.hb[a1][o] += w;
+        hb[a1] += w;
     }
-}
-
-// Transpose of the H update: hb (dF/dH^{n+1/2}) carries over unchanged to
-// H^{n-1/2}; its share through the curl of E goes to t1, t2.
-template <typename real>
-__global__ void __launch_bounds__(AX * AY) k_adj_h(const __grid_constant__ AdjDev<real> A) {
-    const InstDev<real>& I = A.I;
-    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
-    if (i >= I.nx || j >= I.ny) return;
-    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
-    const int idx[3] = {i, j, k};
     for (int ca = 0; ca < 3; ++ca) {
+        A.hb[ca][o] = hb[ca];
         const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
         const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
-        const real cv = -I.S * A.hb[ca][o];
+        const real cv = -I.S * hb[ca];
         real t1 = cv, t2 = -cv;
         if (in_slab(I, a1, idx[a1])) {
             real* ps = A.psHb[a1] + (long long)s1 * I.vol + o;
@@ -143,8 +140,8 @@ __global__ void __launch_bounds__(AX * AY) k_adj_h(const __grid_constant__ AdjDe
             t2 = -cv + prof_at(I, a2, idx[a2], 3) * t;
             *ps = prof_at(I, a2, idx[a2], 2) * t;
         }
-        A.t1[ca][o] = t1;  // adjoint of E_a2(o + e_a1) - E_a2(o)
-        A.t2[ca][o] = t2;  // adjoint of E_a1(o + e_a2) - E_a1(o)
+        A.t3[ca][o] = t1;  // adjoint of E_a2(o + e_a1) - E_a2(o)
+        A.t4[ca][o] = t2;  // adjoint of E_a1(o + e_a2) - E_a1(o)
     }
 }
 
@@ -158,11 +155,11 @@ __global__ void __launch_bounds__(AX * AY) k_adj_h_gather(const __grid_constant_
     const int idx[3] = {i, j, k};
     for (int ca = 0; ca < 3; ++ca) {
         const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
-        real v = -A.t1[ca][o];
-        if (idx[a1] > 0) v += A.t1[ca][o - stride_of(I, a1)];
+        real v = -A.t3[ca][o];
+        if (idx[a1] > 0) v += A.t3[ca][o - stride_of(I, a1)];
         A.eb[a2][o] += v;
-        real w = -A.t2[ca][o];
-        if (idx[a2] > 0) w += A.t2[ca][o - stride_of(I, a2)];
+        real w = -A.t4[ca][o];
+        if (idx[a2] > 0) w += A.t4[ca][o - stride_of(I, a2)];
         A.eb[a1][o] += w;
     }
 }
@@ -197,8 +194,7 @@ template <typename real>
 cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, cudaStream_t s) {
     const dim3 block(AX, AY), grid((a.I.nx + AX - 1) / AX, (a.I.ny + AY - 1) / AY, a.I.nz);
     k_adj_e<real><<<grid, block, 0, s>>>(a, n);
-    k_adj_e_gather<real><<<grid, block, 0, s>>>(a);
-    k_adj_h<real><<<grid, block, 0, s>>>(a);
+    k_adj_e_gather_h<real><<<grid, block, 0, s>>>(a);
     k_adj_h_gather<real><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
 }

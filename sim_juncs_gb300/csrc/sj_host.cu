@@ -1403,6 +1403,8 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
             a.hb[c] = (real*)tmp(vb);
             a.t1[c] = (real*)tmp(vb);
             a.t2[c] = (real*)tmp(vb);
+            a.t3[c] = (real*)tmp(vb);
+            a.t4[c] = (real*)tmp(vb);
         }
         for (int ax = 0; ax < 3; ++ax)
             if (I.psiE[ax]) a.psEb[ax] = (real*)tmp(2 * vb), a.psHb[ax] = (real*)tmp(2 * vb);

@@ -206,8 +206,10 @@ struct AdjDev {
     InstDev<real> I;            // coefficients, geometry, design region
     real* eb[3];                // dF/dE
     real* hb[3];                // dF/dH
-    real* t1[3];                // per component: adjoint of its first difference
+    real* t1[3];                // per component: adjoint of its first difference (E update)
     real* t2[3];                // ... and of its second
+    real* t3[3];                // the same for the H update's differences
+    real* t4[3];
     real* psEb[3];              // [axis] -> [2 slots][vol] (null where the axis has no slab)
     real* psHb[3];
     real* pb;                   // polarisation layout: level 0 = dF/dP^n, level 1 = dF/dP^{n-1}
