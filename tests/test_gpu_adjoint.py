@@ -146,3 +146,28 @@ def test_torch_autograd_binding(lib):
     F2, g2 = g.adjoint_gradient(obj, N_STEPS, checkpoint_every=60)
     assert float(F.detach()) == F2[0]
     np.testing.assert_allclose(eps.grad.numpy(), g2[0], rtol=1e-6, atol=0)
+
+
+def test_design_on_one_member_splits_its_launch_group(lib):
+    # three 64^3 junctions share launches; a design region on the middle one
+    # moves its design tiles to the general class, so the group splits into
+    # runs with equal tile lists; every instance still steps bit for bit as
+    # it does alone
+    from sim_juncs_gb300.configs import junction_instance
+    insts = [junction_instance(n=64, res=20.0, phase=ph, amplitude=a) for ph, a in ((0.2, 1.0), (1.3, 0.5), (2.9, 2.0))]
+    lo = (28, 28, 31)
+    eps = np.random.default_rng(3).uniform(1.0, 4.0, size=(2, 6, 8))
+    des = Design(lo, eps)
+    f = Fields(insts, "f32")
+    grouped = f.launches_per_step()
+    f.set_design(des, 1)
+    assert f.launches_per_step() > grouped
+    f.step(90)
+    for q, inst in enumerate(insts):
+        s = Fields(inst, "f32")
+        if q == 1:
+            s.set_design(des)
+        s.step(90)
+        for c in range(6):
+            np.testing.assert_array_equal(f.get_array(c, q), s.get_array(c), err_msg=f"instance {q} component {c}")
+        s.close()
