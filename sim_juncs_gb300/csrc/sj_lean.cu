@@ -15,9 +15,9 @@
 // The host sorts the tiles into one list per class, by what a tile's
 // footprint (own cells and the x-1/y-1/z-1 neighbours) touches:
 //   plain   (k_lean_plain2 / k_lean_plain): no CPML slab and no H source.
-//           Two columns per thread where rows are whole (nx % 32 == 0): x-1
-//           H from the neighbouring lane by shuffle, y-1 H recomputed from
-//           L1/L2; otherwise one column per thread recomputing both.
+//           Where rows are whole (nx % 32 == 0): the two-column shared-halo
+//           body below with no CPML axis; otherwise one column per thread
+//           recomputing the x-1 and y-1 H from L1/L2.
 //   slab    (k_lean_slab2 / k_lean_slab): the CPML slabs of one axis; multi
 //           (k_lean_multi2 / k_lean_multi): of two or three.  Shared halo:
 //           warps for the row below the tile and the column left of it
@@ -74,9 +74,9 @@ constexpr int LMAXF = 256;
 #endif
 template <typename real>
 constexpr int plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PLAIN_MINB : 3; }
-// the two-column plain kernel's 128-thread blocks
+// the two-column plain kernel's 160-thread blocks
 template <typename real>
-constexpr int pair_plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PAIR_PLAIN_MINB : 4; }
+constexpr int pair_plain_minb() { return sizeof(real) == 4 ? SJ_LEAN_PAIR_PLAIN_MINB : 2; }
 
 template <typename real>
 constexpr int slab_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB_MINB : 2; }
@@ -271,7 +271,7 @@ __device__ __forceinline__ void plain_block(const InstDev<real>& I, int tx, int 
     }
 }
 
-// Vector pairs for the two-column tile body (tile_pair, below).
+// Vector pairs for the two-column tile bodies.
 template <typename real>
 struct Pair;
 template <>
@@ -1092,253 +1092,7 @@ __device__ __forceinline__ void tile_pair_halo_any(const InstDev<real>& I, int t
         tile_pair_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh, qf);
 }
 
-template <typename real>
-__device__ __forceinline__ typename Pair<real>::T ld2z(const real* p, unsigned o, bool ok) {
-    typename Pair<real>::T v;
-    if (ok) return ld2(p, o);
-    v.x = v.y = real(0);
-    return v;
-}
 
-// Two columns per thread (instances whose nx is a multiple of 32, so every
-// pair of a row exists): a half-warp of 16 lanes covers one 32-column row
-// (lane l: columns 2l and 2l+1) and a block of 4 warps the tile's 8 rows.
-// Fields move as pairs (float2 / double2); the H at x-1 that the E update
-// needs comes from the neighbouring lane by shuffle instead of being
-// recomputed, lane 0 recomputes it for the column left of the tile and lane
-// 15 loads the E right of it.  CPML on the axes in MASK (MASK = 0: plain
-// tiles).  Each voxel evaluates tile_block's formulas through the same
-// pml_term calls in the same order, so both bodies give the same bits.
-// Rows beyond ny (EDGE only) run with a clamped row and store nothing, so
-// that every lane reaches the shuffles.
-template <typename real, int ZB, int MASK, bool EDGE>
-__device__ __forceinline__ void tile_pair(const InstDev<real>& I, int tx, int ty, int tz, bool dry, unsigned qf) {
-    using V2 = typename Pair<real>::T;
-    constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
-    const int lane = threadIdx.x & 15, half = threadIdx.x >> 4;
-    const int i = tx * LX + 2 * lane;
-    const int jr = ty * LY + threadIdx.y * 2 + half;
-    const bool act = !EDGE || jr < I.ny;
-    const int j = act ? jr : I.ny - 1;
-    const int z0 = tz * ZB, z1 = min(I.nz, z0 + ZB);
-    const int nx = I.nx, ny = I.ny, nz = I.nz;
-    const unsigned px = (unsigned)I.px, plane = (unsigned)I.plane, vol = (unsigned)I.vol;
-    const real* eX = I.F[0][0];
-    const real* eY = I.F[0][1];
-    const real* eZ = I.F[0][2];
-    const real* hX = I.F[0][3];
-    const real* hY = I.F[0][4];
-    const real* hZ = I.F[0][5];
-    real* oEX = I.F[1][0];
-    real* oEY = I.F[1][1];
-    real* oEZ = I.F[1][2];
-    real* oHX = I.F[1][3];
-    real* oHY = I.F[1][4];
-    real* oHZ = I.F[1][5];
-    // psi bases moved by qf: with the field offsets (which include qf) they
-    // reach group member blockIdx.y's psi at + 2 qf
-    const real* hiX = SX ? I.psiH[0][0] + qf : nullptr;
-    const real* hiY = SY ? I.psiH[0][1] + qf : nullptr;
-    const real* hiZ = SZ ? I.psiH[0][2] + qf : nullptr;
-    real* hoX = SX ? I.psiH[1][0] + qf : nullptr;
-    real* hoY = SY ? I.psiH[1][1] + qf : nullptr;
-    real* hoZ = SZ ? I.psiH[1][2] + qf : nullptr;
-    real* peX = SX ? I.psiE[0] + qf : nullptr;
-    real* peY = SY ? I.psiE[1] + qf : nullptr;
-    real* peZ = SZ ? I.psiE[2] + qf : nullptr;
-    const real S = I.S;
-
-    const bool xm = !EDGE || i > 0, xp1 = !EDGE || i + 2 < nx;
-    const bool ym = !EDGE || j > 0, yp = !EDGE || j + 1 < ny;
-    const bool hm = lane == 0 && xm, hp = lane == 15 && xp1;
-    // slab membership: both columns, the halo column left of the tile, the row and the row below
-    const bool xo0 = SX && in_slab(I, 0, i), xo1 = SX && in_slab(I, 0, i + 1);
-    const bool xoh = SX && hm && in_slab(I, 0, i - 1);
-    const bool yo = SY && in_slab(I, 1, j), yo_m = SY && ym && in_slab(I, 1, j - 1);
-    real bxi0 = 1, cxi0 = 0, bxh0 = 1, cxh0 = 0, bxi1 = 1, cxi1 = 0, bxh1 = 1, cxh1 = 0, bxhh = 1, cxhh = 0;
-    real byi = 1, cyi = 0, byh = 1, cyh = 0, byhm = 1, cyhm = 0;
-    if (SX) {
-        const real* pr = I.prof[0];
-        if (xo0) bxi0 = ldg(pr, i), cxi0 = ldg(pr, nx + i), bxh0 = ldg(pr, 2 * nx + i), cxh0 = ldg(pr, 3 * nx + i);
-        if (xo1)
-            bxi1 = ldg(pr, i + 1), cxi1 = ldg(pr, nx + i + 1), bxh1 = ldg(pr, 2 * nx + i + 1),
-            cxh1 = ldg(pr, 3 * nx + i + 1);
-        if (xoh) bxhh = ldg(pr, 2 * nx + i - 1), cxhh = ldg(pr, 3 * nx + i - 1);
-    }
-    if (SY) {
-        const real* pr = I.prof[1];
-        if (yo) byi = ldg(pr, j), cyi = ldg(pr, ny + j), byh = ldg(pr, 2 * ny + j), cyh = ldg(pr, 3 * ny + j);
-        if (yo_m) byhm = ldg(pr, 2 * ny + j - 1), cyhm = ldg(pr, 3 * ny + j - 1);
-    }
-
-    int k = z0 > 0 ? z0 - 1 : 0;
-    unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i + qf;  // group member blockIdx.y
-    V2 ex_c = ld2(eX, o), ey_c = ld2(eY, o), eym_c = ld2z(eY, o - px, ym);
-    real exm_c = hm ? ldg(eX, o - 1) : real(0);
-    V2 hxp, hyp;
-    hxp.x = hxp.y = hyp.x = hyp.y = real(0);
-    const unsigned orow = o - 2 * lane;  // row start of this half-warp at plane k
-    const int k0 = k;
-    const int i0 = tx * LX;
-    const bool xt = SX && (max(i0 - 1, 0) < I.pl[0] || min(i0 + LX, nx) - 1 >= nx - I.ph[0]);
-    // a half-warp's 16 lanes take rows 0-15 (three-axis tiles: the z psi rows go without)
-    volatile unsigned long long* lr = lane_row_park(lane_row<real, SX, SY, SZ>(I, lane, xt, yo, qf));
-    for (; k < z1; ++k, o += plane) {
-        const bool kp = !EDGE || k + 1 < nz;
-        const bool store = k >= z0;
-        const bool zo = SZ && (k < I.pl[2] || k >= nz - I.ph[2]);
-        if (LEAN_PF > 0) {
-            const int kq = k + 1 + LEAN_PF;
-            prefetch_lane_row<real>(lr, orow + (unsigned)(kq - k0) * plane, act && kq < nz && k + LEAN_PF < z1,
-                              SZ && (kq < I.pl[2] || kq >= nz - I.ph[2]));
-        }
-        real bzi = 1, czi = 0, bzh = 1, czh = 0;
-        if (zo) {
-            const real* pr = I.prof[2];
-            bzi = ldg(pr, k), czi = ldg(pr, nz + k), bzh = ldg(pr, 2 * nz + k), czh = ldg(pr, 3 * nz + k);
-        }
-        const V2 ex_n = ld2z(eX, o + plane, kp), ey_n = ld2z(eY, o + plane, kp);
-        const V2 eym_n = ld2z(eY, o + plane - px, kp && ym);
-        const real exm_n = (hm && kp) ? ldg(eX, o + plane - 1) : real(0);
-        const V2 ez = ld2(eZ, o), ez_yp = ld2z(eZ, o + px, yp), ex_yp = ld2z(eX, o + px, yp);
-        real ez_x2 = __shfl_down_sync(FULL, ez.x, 1, 16), ey_x2 = __shfl_down_sync(FULL, ey_c.x, 1, 16);
-        const real ez_x2l = hp ? ldg(eZ, o + 2) : real(0), ey_x2l = hp ? ldg(eY, o + 2) : real(0);
-        if (lane == 15) ez_x2 = ez_x2l, ey_x2 = ey_x2l;
-        const V2 h_x = ld2(hX, o), h_y = ld2(hY, o), h_z = ld2(hZ, o);
-        const bool sp = store && !dry && act;
-
-        V2 hx, hy, hz;
-        {
-            real d1 = ez_yp.x - ez.x, d2 = ey_n.x - ey_c.x, cv = d1 - d2;
-            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o, sp);
-            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o, sp);
-            hx.x = fma(-S, cv, h_x.x);
-            d1 = ez_yp.y - ez.y, d2 = ey_n.y - ey_c.y, cv = d1 - d2;
-            pml_term<SY, true, true>(cv, yo, byh, cyh, d1, hiY, hoY, o + 1, sp);
-            pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, o + 1, sp);
-            hx.y = fma(-S, cv, h_x.y);
-        }
-        {
-            real d1 = ex_n.x - ex_c.x, d2 = ez.y - ez.x, cv = d1 - d2;
-            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o, sp);
-            pml_term<SX, false, true>(cv, xo0, bxh0, cxh0, d2, hiX, hoX, o, sp);
-            hy.x = fma(-S, cv, h_y.x);
-            d1 = ex_n.y - ex_c.y, d2 = ez_x2 - ez.y, cv = d1 - d2;
-            pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, o + 1, sp);
-            pml_term<SX, false, true>(cv, xo1, bxh1, cxh1, d2, hiX, hoX, o + 1, sp);
-            hy.y = fma(-S, cv, h_y.y);
-        }
-        {
-            real d1 = ey_c.y - ey_c.x, d2 = ex_yp.x - ex_c.x, cv = d1 - d2;
-            pml_term<SX, true, true>(cv, xo0, bxh0, cxh0, d1, hiX + vol, hoX + vol, o, sp);
-            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o, sp);
-            hz.x = fma(-S, cv, h_z.x);
-            d1 = ey_x2 - ey_c.y, d2 = ex_yp.y - ex_c.y, cv = d1 - d2;
-            pml_term<SX, true, true>(cv, xo1, bxh1, cxh1, d1, hiX + vol, hoX + vol, o + 1, sp);
-            pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, o + 1, sp);
-            hz.y = fma(-S, cv, h_z.y);
-        }
-        if (store) {
-            // H at x-1 (Hy, Hz): the previous lane's second column; lane 0 recomputes it
-            real hy_m = __shfl_up_sync(FULL, hy.y, 1, 16), hz_m = __shfl_up_sync(FULL, hz.y, 1, 16);
-            {
-                const unsigned om = o - 1;
-                const real ez_m = hm ? ldg(eZ, om) : real(0), ey_m = hm ? ldg(eY, om) : real(0);
-                const real exyp_m = (hm && yp) ? ldg(eX, om + px) : real(0);
-                real hy_l = 0, hz_l = 0;
-                if (hm) {
-                    real d1 = exm_n - exm_c, d2 = ez.x - ez_m, cv = d1 - d2;
-                    pml_term<SZ, true, true>(cv, zo, bzh, czh, d1, hiZ + vol, hoZ + vol, om, false);
-                    pml_term<SX, false, true>(cv, xoh, bxhh, cxhh, d2, hiX, hoX, om, false);
-                    hy_l = fma(-S, cv, ldg(hY, om));
-                    d1 = ey_c.x - ey_m, d2 = exyp_m - exm_c, cv = d1 - d2;
-                    pml_term<SX, true, true>(cv, xoh, bxhh, cxhh, d1, hiX + vol, hoX + vol, om, false);
-                    pml_term<SY, false, true>(cv, yo, byh, cyh, d2, hiY + vol, hoY + vol, om, false);
-                    hz_l = fma(-S, cv, ldg(hZ, om));
-                }
-                if (lane == 0) hy_m = hy_l, hz_m = hz_l;
-            }
-            // H at y-1 (Hx, Hz), recomputed
-            const unsigned oy = o - px;
-            const V2 ez_ym = ld2z(eZ, oy, ym), ex_ym = ld2z(eX, oy, ym);
-            real eym_x2 = __shfl_down_sync(FULL, eym_c.x, 1, 16);
-            const real eym_x2l = (hp && ym) ? ldg(eY, oy + 2) : real(0);
-            if (lane == 15) eym_x2 = eym_x2l;
-            const V2 hx_y = ld2z(hX, oy, ym), hz_y = ld2z(hZ, oy, ym);
-            V2 hx_ym, hz_ym;
-            hx_ym.x = hx_ym.y = hz_ym.x = hz_ym.y = real(0);
-            if (ym) {
-                real d1 = ez.x - ez_ym.x, d2 = eym_n.x - eym_c.x, cv = d1 - d2;
-                pml_term<SY, true, true>(cv, yo_m, byhm, cyhm, d1, hiY, hoY, oy, false);
-                pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, oy, false);
-                hx_ym.x = fma(-S, cv, hx_y.x);
-                d1 = ez.y - ez_ym.y, d2 = eym_n.y - eym_c.y, cv = d1 - d2;
-                pml_term<SY, true, true>(cv, yo_m, byhm, cyhm, d1, hiY, hoY, oy + 1, false);
-                pml_term<SZ, false, true>(cv, zo, bzh, czh, d2, hiZ, hoZ, oy + 1, false);
-                hx_ym.y = fma(-S, cv, hx_y.y);
-                d1 = eym_c.y - eym_c.x, d2 = ex_c.x - ex_ym.x, cv = d1 - d2;
-                pml_term<SX, true, true>(cv, xo0, bxh0, cxh0, d1, hiX + vol, hoX + vol, oy, false);
-                pml_term<SY, false, true>(cv, yo_m, byhm, cyhm, d2, hiY + vol, hoY + vol, oy, false);
-                hz_ym.x = fma(-S, cv, hz_y.x);
-                d1 = eym_x2 - eym_c.y, d2 = ex_c.y - ex_ym.y, cv = d1 - d2;
-                pml_term<SX, true, true>(cv, xo1, bxh1, cxh1, d1, hiX + vol, hoX + vol, oy + 1, false);
-                pml_term<SY, false, true>(cv, yo_m, byhm, cyhm, d2, hiY + vol, hoY + vol, oy + 1, false);
-                hz_ym.y = fma(-S, cv, hz_y.y);
-            }
-            if (act) {
-                st2(oHX, o, hx.x, hx.y);
-                st2(oHY, o, hy.x, hy.y);
-                st2(oHZ, o, hz.x, hz.y);
-            }
-            const uchar2 cb = __ldg(reinterpret_cast<const uchar2*>(I.combo + o));
-            const real* c0 = I.coef + (int)cb.x * I.ncoef;
-            const real* c1 = I.coef + (int)cb.y * I.ncoef;
-            const bool si = !dry && act;
-            V2 ex, ey, ezn;
-            {
-                real d1 = hz.x - hz_ym.x, d2 = hy.x - hyp.x, cv = d1 - d2;
-                pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o, si);
-                pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o, si);
-                ex.x = e_new<0>(I, c0, ex_c.x, cv);
-                d1 = hz.y - hz_ym.y, d2 = hy.y - hyp.y, cv = d1 - d2;
-                pml_term<SY, true, false>(cv, yo, byi, cyi, d1, peY, peY, o + 1, si);
-                pml_term<SZ, false, false>(cv, zo, bzi, czi, d2, peZ, peZ, o + 1, si);
-                ex.y = e_new<0>(I, c1, ex_c.y, cv);
-            }
-            {
-                real d1 = hx.x - hxp.x, d2 = hz.x - hz_m, cv = d1 - d2;
-                pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o, si);
-                pml_term<SX, false, false>(cv, xo0, bxi0, cxi0, d2, peX, peX, o, si);
-                ey.x = e_new<1>(I, c0, ey_c.x, cv);
-                d1 = hx.y - hxp.y, d2 = hz.y - hz.x, cv = d1 - d2;
-                pml_term<SZ, true, false>(cv, zo, bzi, czi, d1, peZ + vol, peZ + vol, o + 1, si);
-                pml_term<SX, false, false>(cv, xo1, bxi1, cxi1, d2, peX, peX, o + 1, si);
-                ey.y = e_new<1>(I, c1, ey_c.y, cv);
-            }
-            {
-                real d1 = hy.x - hy_m, d2 = hx.x - hx_ym.x, cv = d1 - d2;
-                pml_term<SX, true, false>(cv, xo0, bxi0, cxi0, d1, peX + vol, peX + vol, o, si);
-                pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o, si);
-                ezn.x = e_new<2>(I, c0, ez.x, cv);
-                d1 = hy.y - hy.x, d2 = hx.y - hx_ym.y, cv = d1 - d2;
-                pml_term<SX, true, false>(cv, xo1, bxi1, cxi1, d1, peX + vol, peX + vol, o + 1, si);
-                pml_term<SY, false, false>(cv, yo, byi, cyi, d2, peY + vol, peY + vol, o + 1, si);
-                ezn.y = e_new<2>(I, c1, ez.y, cv);
-            }
-            if (act) {
-                st2(oEX, o, ex.x, ex.y);
-                st2(oEY, o, ey.x, ey.y);
-                st2(oEZ, o, ezn.x, ezn.y);
-            }
-        }
-        hxp = hx;
-        hyp = hy;
-        ex_c = ex_n;
-        ey_c = ey_n;
-        eym_c = eym_n;
-        exm_c = exm_n;
-    }
-}
 
 // Monitors (every save_span steps, before the step) and running DFT sums, read
 // from buffer `cur`, which no stepping block writes during the launch.
@@ -1529,24 +1283,14 @@ k_lean_multi2(const __grid_constant__ LeanTable<real> tab) {
 }
 
 // Plain tiles with two columns per thread (instances whose nx is a multiple
-// of 32), 4 warps per tile.  (The CPML tile classes keep one column per
-// thread: their two-column bodies need too many registers for the occupancy
-// the kernels live on.)
-template <typename real, int ZB, int MASK>
-__device__ __forceinline__ void tile_pair_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
-                                              unsigned qf) {
-    if (tile_edge(I, tx, ty, tz, ZB))
-        tile_pair<real, ZB, MASK, true>(I, tx, ty, tz, dry, qf);
-    else
-        tile_pair<real, ZB, MASK, false>(I, tx, ty, tz, dry, qf);
-}
-
+// of 32): the two-column shared-halo body with no CPML axis, 5 warps per tile.
 template <typename real, int ZB>
-__global__ void __launch_bounds__(LX * LY / 2, pair_plain_minb<real>())
+__global__ void __launch_bounds__(HALO2_THREADS, pair_plain_minb<real>())
 k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
+    __shared__ HaloPlane<real> sh[2];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
-    tile_pair_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, blockIdx.y * tab.qvol);
+    tile_pair_halo_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol);
 }
 
 // General tiles (an H source in the footprint) and probe blocks of every
@@ -1751,7 +1495,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     const long long gb = general_blocks(gen, dry);
     long long gtotal = gb;
     for (int p = 0; p < LEAN_FIX_PASSES; ++p) gtotal += fix.count[p];
-    const dim3 block(LX, LY), half(LX, LY / 2), halo(LX, LY + HALO_WARPS), halo2(LX, LY / 2 + 1);
+    const dim3 block(LX, LY), halo(LX, LY + HALO_WARPS), halo2(LX, LY / 2 + 1);
     // descriptor of instance q with the step's parity applied
     auto table = [&](int q) {
         LeanTable<real> t;
@@ -1796,7 +1540,7 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
             k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);              \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
         if (t.n_tiles && pairs)                                                                              \
-            k_lean_plain2<real, Z><<<dim3((unsigned)t.n_tiles, gn), half, 0, sc[LEAN_PLAIN]>>>(t);           \
+            k_lean_plain2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_PLAIN]>>>(t);          \
         if (t.n_tiles && !pairs)                                                                             \
             k_lean_plain<real, Z><<<dim3((unsigned)t.n_tiles, gn), block, 0, sc[LEAN_PLAIN]>>>(t);           \
         break;
