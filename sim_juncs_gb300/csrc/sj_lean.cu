@@ -1237,10 +1237,11 @@ k_lean_multi(const __grid_constant__ LeanTable<real> tab) {
 }
 
 // Single- and multi-slab tiles with two columns per thread (instances whose
-// nx is a multiple of 32), 5 warps per tile.  (The multi-slab body spills a
-// little at 5 blocks per SM and still runs faster than at 4.)
+// nx is a multiple of 32), 5 warps per tile.  The single-slab body fits 64
+// registers without spilling (6 blocks per SM); the multi-slab body spills a
+// little at 5 blocks per SM and still runs faster there than at 4 or 6.
 #ifndef SJ_LEAN_SLAB2_MINB
-#define SJ_LEAN_SLAB2_MINB 5
+#define SJ_LEAN_SLAB2_MINB 6
 #endif
 #ifndef SJ_LEAN_MULTI2_MINB
 #define SJ_LEAN_MULTI2_MINB 5
