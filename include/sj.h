@@ -145,21 +145,36 @@ typedef struct {
     const double* sigma;        /* [n_poles], already divided by thickness */
 } sj_region_desc;
 
-/* cgs_material_function semantics (src/disp.cpp:264-283) with smooth_n = 0.
+/* cgs_material_function semantics (src/disp.cpp:264-283).
    SJ_EPS_SUM (the reference's behaviour):
-     eps(r) = sum_roots [ambient + (s_root - ambient) * in_root(r)]
+     eps(r) = sum_roots [ambient + (s_root - ambient) * f_root(r)]
      (ambient alone when there is no root), so empty space carries
      n_roots * ambient;
    SJ_EPS_FIRST (what the comment at src/disp.cpp:271 describes):
      eps(r) = s of the first root containing r, else ambient.
-   In both modes sigma_{root,q}(r) = sigma * in_root(r), except that under
-   SJ_EPS_FIRST only the first containing root contributes poles. */
+   In both modes sigma_{root,q}(r) = sigma * f_root(r), except that under
+   SJ_EPS_FIRST only the first containing root contributes poles.
+
+   f_root is the fill fraction.  With smooth_n = 0 it is in_root(r) (0/1).
+   With smooth_n > 0 (stochastic smoothing, SJ_EPS_SUM only) it is
+     f_root(r) = (in_root(r) + sum_j in_root(r + d_j)) / (N + 1),
+   N = 8 smooth_n, d_j the offsets sj_smooth_points returns: smooth_n draws
+   of cgs_material_function::generate_smooth_pts (src/disp.cpp:56-112,
+   std::mt19937 seeded as there with DEF_SEED = 0xd9a28bf3, src/disp.hpp:34),
+   each reflected through the 8 octants.  Every Yee point's class is then the
+   tuple of its per-root counts; a scene whose voxels carry more than 256
+   distinct (Ex, Ey, Ez) class triples is rejected (SJ_E_INVALID). */
 enum { SJ_EPS_SUM = 0, SJ_EPS_FIRST = 1 };
+#define SJ_MAX_SMOOTH_N 31
 typedef struct {
     double ambient_eps;
     int32_t n_regions;
     int32_t combine;            /* SJ_EPS_SUM (default) or SJ_EPS_FIRST */
     const sj_region_desc* regions;
+    int32_t smooth_n;           /* 0 = off (the reference's default, src/argparse.h:40);
+                                   1 .. SJ_MAX_SMOOTH_N */
+    double smooth_rad;          /* standard deviation of the radial draw, length units
+                                   (the reference's DEFAULT_SMOOTH_RAD is 0.05) */
 } sj_scene_desc;
 
 /* Material description: either an explicit per-component class map with a
@@ -397,8 +412,17 @@ int sj_objective(sj_sim* sim, const sj_objective_desc* objectives, int64_t n_ste
 /* ---------------------------------------------------------------- rasteriser */
 /* cgs_material_function::in_bound per E-component Yee point, on the device:
    out_masks[3][nz][ny][nx] = bitmask of the scene regions containing the
-   point (composite_object::in, src/cgs.cpp:403-449). */
+   point (composite_object::in, src/cgs.cpp:403-449).  The scene's smooth_n
+   must be 0 (a smoothed scene has fill counts: sj_rasterize_counts). */
 int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out_masks);
+/* The fill counts behind f_root on the device: out_counts[3][n_regions][nz][ny][nx]
+   = in_root(r) + sum_j in_root(r + d_j) at each E-component Yee point
+   (cgs_material_function::in_bound's this_ret, src/disp.cpp:272-279), so
+   0 .. 8 smooth_n + 1; with smooth_n = 0 the region's bit of sj_rasterize. */
+int sj_rasterize_counts(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out_counts);
+/* The smoothing offsets (host): out[8 smooth_n][3], the reflections of each draw
+   in the order of src/disp.cpp:95-104 (x sign outermost).  cap in doubles. */
+int sj_smooth_points(int32_t smooth_n, double smooth_rad, double* out, size_t cap);
 
 /* Allocation-free rasteriser (no counterpart in the reference).
    For callers that cannot allocate device memory: code running while a

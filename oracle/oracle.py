@@ -63,6 +63,10 @@ def load():
     lib.sjo_rasterize.argtypes = [C.POINTER(_abi.GridDesc), C.POINTER(_abi.SceneDesc),
                                   C.POINTER(C.c_uint8)]
     lib.sjo_csg_in.argtypes = [C.POINTER(_abi.CsgNode), C.c_int, D, C.c_int64, C.POINTER(C.c_uint8)]
+    lib.sjo_rasterize_counts.argtypes = [C.POINTER(_abi.GridDesc), C.POINTER(_abi.SceneDesc),
+                                         C.POINTER(C.c_uint8)]
+    lib.sjo_smooth_points.argtypes = [C.c_int32, C.c_double, D]
+    lib.sjo_in_bound.argtypes = [C.POINTER(_abi.SceneDesc), D, C.c_int64, D]
     lib.sjo_set_design.argtypes = [P, C.POINTER(_abi.DesignDesc)]
     lib.sjo_objective.argtypes = [P, C.POINTER(_abi.ObjectiveDesc), C.c_int64, D]
     lib.sjo_adjoint.argtypes = [P, C.POINTER(_abi.ObjectiveDesc), C.c_int64, D, D]
@@ -162,6 +166,41 @@ def rasterize(grid, scene):
     out = np.zeros((3, grid.nz, grid.ny, grid.nx), dtype=np.uint8)
     g = grid.to_c()
     lib.sjo_rasterize(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out
+
+
+def rasterize_counts(grid, scene):
+    """in_bound's per-region counts: [3][n_regions][nz][ny][nx]."""
+    from sim_juncs_gb300.spec import scene_to_c
+    lib = load()
+    sc, h = scene_to_c(scene)
+    out = np.zeros((3, len(scene.regions), grid.nz, grid.ny, grid.nx), dtype=np.uint8)
+    g = grid.to_c()
+    rc = lib.sjo_rasterize_counts(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    if rc:
+        raise RuntimeError(lib.sjo_last_error().decode())
+    return out
+
+
+def smooth_points(n, rad):
+    """The smoothing offsets: [8 n][3]."""
+    lib = load()
+    out = np.zeros((8 * n, 3), dtype=np.float64)
+    lib.sjo_smooth_points(n, rad, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def in_bound(scene, points):
+    """cgs_material_function::in_bound of the scene's eps at each point."""
+    from sim_juncs_gb300.spec import scene_to_c
+    lib = load()
+    sc, h = scene_to_c(scene)
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    out = np.zeros(len(pts), dtype=np.float64)
+    rc = lib.sjo_in_bound(sc, pts.ctypes.data_as(C.POINTER(C.c_double)), len(pts),
+                          out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc:
+        raise RuntimeError(lib.sjo_last_error().decode())
     return out
 
 

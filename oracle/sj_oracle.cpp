@@ -13,10 +13,11 @@
  *     quadratic profile, R = 1e-15, meep's defaults), and meep's Lorentzian /
  *     Drude polarisation update (lorentzian_susceptibility, added per root and
  *     pole at src/disp.cpp:529-548);
- *   - cgs_material_function::in_bound (src/disp.cpp:264-283) with
- *     smooth_n = 0, over composite_object::in and the primitives' in()
- *     (src/cgs.cpp:34-120, 403-449), evaluated in the reference's operation
- *     order;
+ *   - cgs_material_function::in_bound (src/disp.cpp:264-283), over
+ *     composite_object::in and the primitives' in() (src/cgs.cpp:34-120,
+ *     403-449), evaluated in the reference's operation order, with the
+ *     stochastic smoothing samples of generate_smooth_pts (src/disp.cpp:56-112)
+ *     when the scene's smooth_n > 0;
  *   - gaussian_src_time_phase (src/disp.cpp:378-400) and the current
  *     (d(t) - d(t - dt)) / dt injected through add_volume_source
  *     (src/disp.cpp:614).
@@ -32,6 +33,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <random>
 #include <string>
 #include <vector>
 #include <omp.h>
@@ -131,6 +133,56 @@ int program_in(const sj_csg_node* nodes, int n, double x, double y, double z) {
     return stk.empty() ? 0 : stk.back();
 }
 
+// generate_smooth_pts (src/disp.cpp:56-112) as the cgs_material_function
+// constructors call it, seed DEF_SEED (src/disp.hpp:34: the double
+// 0xd9a28bf3, converted to uint64_t); the seed_seq words are seed & 0xffff
+// and (seed & 0xffff0000) >> 32, which is 0.  Returns the 8 n reflected
+// offsets, 3 doubles each.
+std::vector<double> smooth_offsets(int n, double rad) {
+    const unsigned long long seed = 0xd9a28bf3ull;
+    std::seed_seq seq{(unsigned)(seed & 0xffffull), (unsigned)((seed & 0xffff0000ull) >> 32)};
+    std::mt19937 eng(seq);
+    std::normal_distribution<double> gauss(0.0, rad);
+    std::uniform_real_distribution<double> uni(0.0, 1.0);
+    std::vector<double> pts;
+    for (int q = 0; q < n; ++q) {
+        const double ti = uni(eng);                       // theta_inv
+        const double cth = 1 - 2 * ti;
+        const double sth = 2 * sqrt(ti * (1 - ti));
+        const double ph = 2 * M_PI * uni(eng);
+        const double rr = gauss(eng);
+        const double v[3] = {rr * sth * cos(ph), rr * sth * cos(ph), rr * cth};  // y as written there
+        for (int a = 0; a < 8; ++a) {                     // signs: x outermost, z innermost
+            pts.push_back((a & 4) ? v[0] : -v[0]);
+            pts.push_back((a & 2) ? v[1] : -v[1]);
+            pts.push_back((a & 1) ? v[2] : -v[2]);
+        }
+    }
+    return pts;
+}
+
+// in_bound's this_ret of each region at (x, y, z), 8 bits per region
+unsigned long long point_counts(const sj_scene_desc* sc, const std::vector<double>& offs, double x, double y,
+                                double z) {
+    unsigned long long key = 0;
+    const size_t n = offs.size() / 3;
+    for (int r = 0; r < sc->n_regions; ++r) {
+        const sj_region_desc& rg = sc->regions[r];
+        unsigned cnt = (unsigned)program_in(rg.nodes, rg.n_nodes, x, y, z);
+        for (size_t q = 0; q < n; ++q)
+            cnt += (unsigned)program_in(rg.nodes, rg.n_nodes, x + offs[3 * q], y + offs[3 * q + 1], z + offs[3 * q + 2]);
+        key |= (unsigned long long)cnt << (8 * r);
+    }
+    return key;
+}
+
+std::vector<double> scene_offsets(const sj_scene_desc* sc) {
+    if (sc->smooth_n < 0 || sc->smooth_n > SJ_MAX_SMOOTH_N) throw std::string("bad smooth_n");
+    if (sc->smooth_n == 0) return {};
+    if (!(sc->smooth_rad > 0)) throw std::string("bad smooth_rad");
+    return smooth_offsets(sc->smooth_n, sc->smooth_rad);
+}
+
 // ---------------------------------------------------------------- oracle state
 struct Src {
     sj_source_desc d;
@@ -222,6 +274,42 @@ void build(sjo_sim* s, const sj_instance_desc& d) {
                 poles.push_back(sc->regions[r].poles[q]);
                 owner.push_back({r, sc->regions[r].sigma[q]});
             }
+        const std::vector<double> offs = scene_offsets(sc);
+        if (!offs.empty()) {
+            // smoothed: class = the point's tuple of counts (sorted distinct tuples)
+            if (sc->combine != SJ_EPS_SUM) throw std::string("smoothing needs SJ_EPS_SUM");
+            std::vector<unsigned long long> keys(3 * s->N);
+#pragma omp parallel for schedule(dynamic)
+            for (int k = 0; k < s->nz; ++k)
+                for (int j = 0; j < s->ny; ++j)
+                    for (int i = 0; i < s->nx; ++i)
+                        for (int c = 0; c < 3; ++c) {
+                            const double x = g.origin[0] + ((double)i + (c == 0 ? 0.5 : 0.0)) * g.dx;
+                            const double y = g.origin[1] + ((double)j + (c == 1 ? 0.5 : 0.0)) * g.dx;
+                            const double z = g.origin[2] + ((double)k + (c == 2 ? 0.5 : 0.0)) * g.dx;
+                            keys[c * s->N + s->at(i, j, k)] = point_counts(sc, offs, x, y, z);
+                        }
+            std::vector<unsigned long long> uniq(keys);
+            std::sort(uniq.begin(), uniq.end());
+            uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+            if (uniq.size() > 256) throw std::string("more than 256 smoothed point classes");
+            ncls = (int)uniq.size();
+            for (int c = 0; c < 3; ++c)
+                for (long long q = 0; q < s->N; ++q)
+                    s->cls[c][q] = (uint8_t)(std::lower_bound(uniq.begin(), uniq.end(), keys[c * s->N + q]) - uniq.begin());
+            const double n1 = (double)(offs.size() / 3 + 1);   // smooth_n + 1 after the x8
+            eps.assign(ncls, 0.0);
+            sigma.assign((size_t)ncls * poles.size(), 0.0);
+            for (int mm = 0; mm < ncls; ++mm) {
+                double ret = 0;
+                for (int r = 0; r < R; ++r)
+                    ret += sc->ambient_eps + (sc->regions[r].eps - sc->ambient_eps) * (double)((uniq[mm] >> (8 * r)) & 255) / n1;
+                eps[mm] = R == 0 ? sc->ambient_eps : ret;
+                for (size_t p = 0; p < poles.size(); ++p)
+                    sigma[(size_t)mm * poles.size() + p] =
+                        0.0 + (owner[p].second - 0.0) * (double)((uniq[mm] >> (8 * owner[p].first)) & 255) / n1;
+            }
+        } else {
         eps.assign(ncls, 0.0);
         sigma.assign((size_t)ncls * poles.size(), 0.0);
         for (int mm = 0; mm < ncls; ++mm) {
@@ -261,6 +349,7 @@ void build(sjo_sim* s, const sj_instance_desc& d) {
                         }
                         s->cls[c][s->at(i, j, k)] = (uint8_t)mask;
                     }
+        }
     }
     s->inv_eps.resize(ncls);
     for (int c = 0; c < ncls; ++c) s->inv_eps[c] = 1.0 / eps[c];
@@ -792,6 +881,64 @@ int sjo_rasterize(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* out) 
                         if (program_in(sc->regions[r].nodes, sc->regions[r].n_nodes, x, y, z)) mask |= 1u << r;
                     out[c * N + ((long long)k * g->ny + j) * g->nx + i] = (uint8_t)mask;
                 }
+    return SJ_OK;
+}
+
+// in_bound's per-region counts at the E points: out[3][R][nz][ny][nx]
+int sjo_rasterize_counts(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* out) {
+    std::vector<double> offs;
+    try {
+        offs = scene_offsets(sc);
+    } catch (const std::string& e) {
+        g_err = e;
+        return SJ_E_INVALID;
+    }
+    const long long N = (long long)g->nx * g->ny * g->nz;
+    const int R = sc->n_regions;
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j)
+            for (int i = 0; i < g->nx; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    const double x = g->origin[0] + ((double)i + (c == 0 ? 0.5 : 0.0)) * g->dx;
+                    const double y = g->origin[1] + ((double)j + (c == 1 ? 0.5 : 0.0)) * g->dx;
+                    const double z = g->origin[2] + ((double)k + (c == 2 ? 0.5 : 0.0)) * g->dx;
+                    const unsigned long long key = point_counts(sc, offs, x, y, z);
+                    const long long q = ((long long)k * g->ny + j) * g->nx + i;
+                    for (int r = 0; r < R; ++r) out[((long long)c * R + r) * N + q] = (uint8_t)((key >> (8 * r)) & 255);
+                }
+    return SJ_OK;
+}
+
+// the smoothing offsets: out[8 n][3]
+int sjo_smooth_points(int32_t n, double rad, double* out) {
+    const std::vector<double> p = smooth_offsets(n, rad);
+    std::copy(p.begin(), p.end(), out);
+    return SJ_OK;
+}
+
+// cgs_material_function::in_bound (src/disp.cpp:264-283) at arbitrary points,
+// the scene's smoothing included: out[n]
+int sjo_in_bound(const sj_scene_desc* sc, const double* pts, int64_t n, double* out) {
+    std::vector<double> offs;
+    try {
+        offs = scene_offsets(sc);
+    } catch (const std::string& e) {
+        g_err = e;
+        return SJ_E_INVALID;
+    }
+    const double n1 = (double)(offs.size() / 3 + 1);
+    for (int64_t q = 0; q < n; ++q) {
+        const unsigned long long key = point_counts(sc, offs, pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+        if (sc->n_regions == 0) {
+            out[q] = sc->ambient_eps;
+            continue;
+        }
+        double ret = 0;
+        for (int r = 0; r < sc->n_regions; ++r)
+            ret += sc->ambient_eps + (sc->regions[r].eps - sc->ambient_eps) * (double)((key >> (8 * r)) & 255) / n1;
+        out[q] = ret;
+    }
     return SJ_OK;
 }
 

@@ -53,7 +53,7 @@ class RegionDesc(C.Structure):
 
 class SceneDesc(C.Structure):
     _fields_ = [("ambient_eps", C.c_double), ("n_regions", C.c_int32), ("combine", C.c_int32),
-                ("regions", C.POINTER(RegionDesc))]
+                ("regions", C.POINTER(RegionDesc)), ("smooth_n", C.c_int32), ("smooth_rad", C.c_double)]
 
 
 class MaterialDesc(C.Structure):
@@ -147,6 +147,8 @@ SIGNATURES = {
     "sj_read_class_map": (C.c_int, [_P, C.c_int32, _U8, C.c_size_t]),
     "sj_max_abs_e": (C.c_int, [_P, C.c_int32, _D]),
     "sj_rasterize": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _U8]),
+    "sj_rasterize_counts": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _U8]),
+    "sj_smooth_points": (C.c_int, [C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_size_t]),
     "sj_rasterize_static": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _P, _P]),
     "sj_source_dipole": (C.c_int, [C.POINTER(SourceDesc), C.c_double, _D, _D]),
     "sj_source_current": (C.c_int, [C.POINTER(SourceDesc), C.c_double, C.c_double, _D, _D]),

@@ -17,8 +17,9 @@ HEADERS = ["sj_internal.h", "sj_physics.cuh", os.path.join("..", "..", "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # the fused stepper writes every fused multiply-add explicitly (results must
-# not depend on which of its kernels updated a voxel)
-FILE_FLAGS = {"sj_lean.cu": ["-fmad=false"]}
+# not depend on which of its kernels updated a voxel); host tables and the
+# smoothing offsets are computed without contraction on every host CPU
+FILE_FLAGS = {"sj_lean.cu": ["-fmad=false"], "sj_host.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc():

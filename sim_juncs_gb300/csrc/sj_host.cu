@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -271,6 +272,12 @@ void check_scene(const sj_scene_desc* sc) {
         total += g.n_nodes;
     }
     if (total > SJ_MAX_CSG_NODES * SJ_MAX_REGIONS) fail(SJ_E_INVALID, "too many CSG nodes");
+    if (sc->smooth_n < 0 || sc->smooth_n > SJ_MAX_SMOOTH_N) fail(SJ_E_INVALID, "scene smooth_n must be in [0, 31]");
+    if (sc->smooth_n > 0) {
+        if (!(sc->smooth_rad > 0) || !std::isfinite(sc->smooth_rad))
+            fail(SJ_E_INVALID, "scene smooth_rad must be finite and > 0");
+        if (sc->combine != SJ_EPS_SUM) fail(SJ_E_INVALID, "smoothing needs the SJ_EPS_SUM combine mode");
+    }
 }
 
 void upload_scene(sj_sim* sim, const sj_scene_desc* sc, sj_csg_node** d_nodes, int** d_start) {
@@ -327,6 +334,118 @@ void scene_classes(const sj_scene_desc* sc, std::vector<double>& eps, std::vecto
     }
 }
 
+// Smoothing offsets: cgs_material_function::generate_smooth_pts
+// (src/disp.cpp:56-112) as the constructors call it, with seed DEF_SEED
+// (src/disp.hpp:34, the double 0xd9a28bf3).  Its seed_seq takes the seed's
+// low 16 bits and (bits 16-31) >> 32, i.e. {0x8bf3, 0}.  Per draw: u, then
+// phi = 2 pi u', then the radius r from N(0, smooth_rad); the point is
+// (r sin(theta) cos(phi), the same for y, r cos(theta)) with cos(theta) =
+// 1 - 2u, sin(theta) = 2 sqrt(u (1 - u)), and its 8 sign reflections follow
+// with the x sign outermost.  libstdc++'s generators and distributions give
+// the reference's sequence.
+std::vector<double> smooth_points(int n, double rad) {
+    std::seed_seq seeder{0x8bf3u, 0u};
+    std::mt19937 gen(seeder);
+    std::normal_distribution<double> radial(0.0, rad);
+    std::uniform_real_distribution<double> unit(0.0, 1.0);
+    std::vector<double> out;
+    out.reserve((size_t)24 * n);
+    for (int d = 0; d < n; ++d) {
+        const double u = unit(gen);
+        const double ct = 1 - 2 * u;
+        const double st = 2 * std::sqrt(u * (1 - u));
+        const double phi = 2 * M_PI * unit(gen);
+        const double r = radial(gen);
+        const double x = r * st * std::cos(phi), y = r * st * std::cos(phi), z = r * ct;
+        for (int sx = -1; sx < 2; sx += 2)
+            for (int sy = -1; sy < 2; sy += 2)
+                for (int sz = -1; sz < 2; sz += 2) {
+                    out.push_back(x * sx);
+                    out.push_back(y * sy);
+                    out.push_back(z * sz);
+                }
+    }
+    return out;
+}
+
+// class table of a smoothed scene: class q = sorted key q, key = the point's
+// counts 8 bits per region; in_bound's sum with this_ret = count over
+// smooth_n + 1 = 8 n + 1 samples (src/disp.cpp:272-280), the susceptibility
+// scale functions the same with def_ret 0 (src/disp.cpp:545)
+void smooth_scene_classes(const sj_scene_desc* sc, const std::vector<unsigned long long>& keys,
+                          std::vector<double>& eps, std::vector<sj_pole>& poles, std::vector<double>& sigma,
+                          int& n_classes) {
+    const int R = sc->n_regions;
+    const double samples = (double)(8 * sc->smooth_n + 1);
+    n_classes = (int)keys.size();
+    poles.clear();
+    std::vector<std::pair<int, double>> owner;
+    for (int r = 0; r < R; ++r)
+        for (int q = 0; q < sc->regions[r].n_poles; ++q) {
+            poles.push_back(sc->regions[r].poles[q]);
+            owner.push_back({r, sc->regions[r].sigma[q]});
+        }
+    if ((int)poles.size() > SJ_MAX_POLES) fail(SJ_E_INVALID, "more than 8 susceptibilities in scene");
+    eps.assign(n_classes, 0.0);
+    sigma.assign((size_t)n_classes * poles.size(), 0.0);
+    const double def = sc->ambient_eps;
+    for (int m = 0; m < n_classes; ++m) {
+        if (R == 0) {
+            eps[m] = def;
+        } else {
+            double ret = 0;
+            for (int r = 0; r < R; ++r) {
+                const double cnt = (double)((keys[m] >> (8 * r)) & 255);
+                ret += def + (sc->regions[r].eps - def) * cnt / samples;
+            }
+            eps[m] = ret;
+        }
+        for (size_t p = 0; p < poles.size(); ++p) {
+            const double cnt = (double)((keys[m] >> (8 * owner[p].first)) & 255);
+            sigma[(size_t)m * poles.size() + p] = 0.0 + (owner[p].second - 0.0) * cnt / samples;
+        }
+    }
+}
+
+// Rasterise a smoothed scene into d_cls (pitched [3][cpitch]); returns the
+// sorted distinct keys (the classes).
+std::vector<unsigned long long> smooth_rasterize(sj_sim* sim, const sj_scene_desc* sc, const sj_grid_desc& g,
+                                                 int px, const sj_csg_node* d_nodes, const int* d_start,
+                                                 uint8_t* d_cls, long long cpitch, cudaStream_t st) {
+    const std::vector<double> offs = smooth_points(sc->smooth_n, sc->smooth_rad);
+    double* d_offs = sim->upload(offs);
+    unsigned long long* d_keys = (unsigned long long*)sim->dalloc(3 * cpitch * sizeof(unsigned long long), false);
+    unsigned long long* d_set = (unsigned long long*)sim->dalloc(SMOOTH_SET_CAP * sizeof(unsigned long long), false);
+    int* d_over = (int*)sim->dalloc(sizeof(int));
+    ck(cudaMemsetAsync(d_set, 0xff, SMOOTH_SET_CAP * sizeof(unsigned long long), st), "set clear");
+    ck(launch_rasterize_counts(d_nodes, d_start, sc->n_regions, g.nx, g.ny, g.nz, g.dx, g.origin, d_offs,
+                               (int)(offs.size() / 3), d_keys, cpitch, px, d_set, SMOOTH_SET_CAP, d_over, st),
+       "rasterize counts");
+    std::vector<unsigned long long> set(SMOOTH_SET_CAP);
+    int over = 0;
+    ck(cudaMemcpyAsync(set.data(), d_set, set.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st),
+       "set read");
+    ck(cudaMemcpyAsync(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost, st), "overflow read");
+    ck(cudaStreamSynchronize(st), "smoothing sync");
+    sim->d2h += (long long)(set.size() * sizeof(unsigned long long) + sizeof(int));
+    std::vector<unsigned long long> keys;
+    for (unsigned long long k : set)
+        if (k != ~0ull) keys.push_back(k);
+    std::sort(keys.begin(), keys.end());
+    if (over || keys.size() > 256)
+        fail(SJ_E_INVALID, "smoothing gives more than 256 distinct point classes (lower smooth_n or smooth_rad)");
+    unsigned long long* d_sorted = sim->upload(keys);
+    ck(launch_class_assign(d_keys, cpitch, g.nx, g.ny, g.nz, px, d_sorted, (int)keys.size(), d_cls, st),
+       "class assign");
+    ck(cudaStreamSynchronize(st), "smoothing sync");
+    sim->dfree(d_sorted);
+    sim->dfree(d_over);
+    sim->dfree(d_set);
+    sim->dfree(d_keys);
+    sim->dfree(d_offs);
+    return keys;
+}
+
 // ------------------------------------------------------------------ builder
 template <typename real>
 void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, InstDev<real>& I) {
@@ -379,13 +498,19 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
         sim->h2d += 3ll * nx * ny * nz;
     } else {
         check_scene(m.scene);
-        scene_classes(m.scene, eps, poles, sigma, n_classes);
         sj_csg_node* d_nodes;
         int* d_start;
         upload_scene(sim, m.scene, &d_nodes, &d_start);
-        ck(launch_rasterize(d_nodes, d_start, m.scene->n_regions, nx, ny, nz, H.dx, g.origin, d_cls,
-                            cpitch, px, st),
-           "rasterize");
+        if (m.scene->smooth_n > 0) {
+            const std::vector<unsigned long long> keys =
+                smooth_rasterize(sim, m.scene, g, px, d_nodes, d_start, d_cls, cpitch, st);
+            smooth_scene_classes(m.scene, keys, eps, poles, sigma, n_classes);
+        } else {
+            scene_classes(m.scene, eps, poles, sigma, n_classes);
+            ck(launch_rasterize(d_nodes, d_start, m.scene->n_regions, nx, ny, nz, H.dx, g.origin, d_cls,
+                                cpitch, px, st),
+               "rasterize");
+        }
     }
     for (int c = 0; c < n_classes; ++c)
         if (!(eps[c] != 0.0) || !std::isfinite(eps[c])) fail(SJ_E_INVALID, "eps_inf must be finite and nonzero");
@@ -2013,6 +2138,8 @@ int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* 
         if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0))
             fail(SJ_E_INVALID, "bad grid");
         check_scene(scene);
+        if (scene->smooth_n != 0)
+            fail(SJ_E_INVALID, "a smoothed scene has fill counts, not region masks (sj_rasterize_counts)");
         sj_sim tmp;
         ck(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking), "stream");
         tmp.own_stream = true;
@@ -2030,6 +2157,53 @@ int sj_rasterize(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* 
     } catch (const Fail& f) {
         return finish(nullptr, f.code, f.msg);
     }
+    return SJ_OK;
+}
+
+int sj_rasterize_counts(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* out) {
+    if (!grid || !scene || !out) return finish(nullptr, SJ_E_INVALID, "NULL argument");
+    try {
+        if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0))
+            fail(SJ_E_INVALID, "bad grid");
+        check_scene(scene);
+        sj_sim tmp;
+        ck(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking), "stream");
+        tmp.own_stream = true;
+        sj_csg_node* d_nodes;
+        int* d_start;
+        upload_scene(&tmp, scene, &d_nodes, &d_start);
+        const int nx = grid->nx, ny = grid->ny, nz = grid->nz, R = scene->n_regions;
+        const long long nv = (long long)nx * ny * nz;
+        const std::vector<double> offs =
+            scene->smooth_n > 0 ? smooth_points(scene->smooth_n, scene->smooth_rad) : std::vector<double>();
+        double* d_offs = tmp.upload(offs);
+        unsigned long long* d = (unsigned long long*)tmp.dalloc(3 * nv * sizeof(unsigned long long));
+        ck(launch_rasterize_counts(d_nodes, d_start, R, nx, ny, nz, grid->dx, grid->origin, d_offs,
+                                   (int)(offs.size() / 3), d, nv, nx, nullptr, 0, nullptr, tmp.stream),
+           "rasterize counts");
+        std::vector<unsigned long long> keys(3 * nv);
+        ck(cudaMemcpyAsync(keys.data(), d, keys.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           tmp.stream),
+           "count read");
+        ck(cudaStreamSynchronize(tmp.stream), "sync");
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < R; ++r)
+                for (long long q = 0; q < nv; ++q)
+                    out[((long long)c * R + r) * nv + q] = (uint8_t)((keys[c * nv + q] >> (8 * r)) & 255);
+    } catch (const Fail& f) {
+        return finish(nullptr, f.code, f.msg);
+    }
+    return SJ_OK;
+}
+
+int sj_smooth_points(int32_t smooth_n, double smooth_rad, double* out, size_t cap) {
+    if (!out) return finish(nullptr, SJ_E_INVALID, "NULL argument");
+    if (smooth_n < 0 || smooth_n > SJ_MAX_SMOOTH_N) return finish(nullptr, SJ_E_INVALID, "smooth_n must be in [0, 31]");
+    if (!(smooth_rad > 0) || !std::isfinite(smooth_rad))
+        return finish(nullptr, SJ_E_INVALID, "smooth_rad must be finite and > 0");
+    if ((size_t)24 * smooth_n > cap) return finish(nullptr, SJ_E_RANGE, "out holds fewer than 24 smooth_n doubles");
+    const std::vector<double> p = smooth_points(smooth_n, smooth_rad);
+    std::copy(p.begin(), p.end(), out);
     return SJ_OK;
 }
 

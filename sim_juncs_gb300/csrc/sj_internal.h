@@ -234,6 +234,17 @@ cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_sta
                              int n_regions, int nx, int ny, int nz, double dx,
                              const double* origin, uint8_t* d_masks, long long mask_pitch_elems,
                              int px, cudaStream_t s);
+// smoothing: per-point region counts packed 8 bits per region (keys, pitched
+// [3][pitch]), distinct keys into a set of cap slots, then key -> class byte
+constexpr unsigned SMOOTH_SET_CAP = 4096;
+cudaError_t launch_rasterize_counts(const sj_csg_node* d_nodes, const int* d_region_start, int n_regions,
+                                    int nx, int ny, int nz, double dx, const double* origin,
+                                    const double* d_offs, int n_offs, unsigned long long* d_keys,
+                                    long long key_pitch_elems, int px, unsigned long long* d_set,
+                                    unsigned cap, int* d_overflow, cudaStream_t s);
+cudaError_t launch_class_assign(const unsigned long long* d_keys, long long pitch, int nx, int ny, int nz,
+                                int px, const unsigned long long* d_sorted, int n_keys, uint8_t* d_cls,
+                                cudaStream_t s);
 cudaError_t launch_combo_mark(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
                               int px, uint32_t* d_bitmap, cudaStream_t s);
 cudaError_t launch_combo_assign(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,

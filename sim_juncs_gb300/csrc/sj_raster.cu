@@ -111,6 +111,125 @@ cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_sta
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ smoothing
+// Stochastic smoothing (cgs_material_function::in_bound, src/disp.cpp:264-283):
+// at each E-component Yee point, region g's count is in(r) plus in(r + d_j)
+// over the n_offs offsets, r + d_j formed by one rounded add per axis as there.
+// A point's key packs the counts 8 bits per region (at most 8 * 31 + 1 = 249,
+// so the all-ones word never occurs and marks an empty slot of the key set).
+constexpr unsigned long long SMOOTH_EMPTY = ~0ull;
+
+__device__ __forceinline__ unsigned smooth_slot(unsigned long long key, unsigned cap) {
+    key ^= key >> 29;
+    key *= 0xbf58476d1ce4e5b9ull;
+    key ^= key >> 32;
+    return (unsigned)key & (cap - 1);
+}
+
+// Insert key into the open-addressing set (cap a power of two); at most cap
+// probes, after which *overflow is raised.
+__device__ void smooth_insert(unsigned long long* set, unsigned cap, unsigned long long key, int* overflow) {
+    unsigned h = smooth_slot(key, cap);
+    for (unsigned probe = 0; probe < cap; ++probe) {
+        const unsigned long long cur = ((volatile unsigned long long*)set)[h];
+        if (cur == key) return;
+        if (cur == SMOOTH_EMPTY) {
+            const unsigned long long prev = atomicCAS(set + h, SMOOTH_EMPTY, key);
+            if (prev == SMOOTH_EMPTY || prev == key) return;
+        }
+        h = (h + 1) & (cap - 1);
+    }
+    atomicExch(overflow, 1);
+}
+
+// One thread per voxel: keys of the Ex, Ey and Ez points; with a set, every
+// distinct key also goes into it (one insert per distinct key of a warp).
+__global__ void k_rasterize_counts(const sj_csg_node* __restrict__ nodes, const int* __restrict__ rstart,
+                                   int n_regions, int nx, int ny, int nz, double dx, double ox, double oy,
+                                   double oz, const double* __restrict__ offs, int n_offs,
+                                   unsigned long long* __restrict__ keys, long long kpitch, int px,
+                                   unsigned long long* __restrict__ set, unsigned cap, int* __restrict__ overflow) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    for (int c = 0; c < 3; ++c) {
+        const double x = __dadd_rn(ox, __dmul_rn((double)i + (c == 0 ? 0.5 : 0.0), dx));
+        const double y = __dadd_rn(oy, __dmul_rn((double)j + (c == 1 ? 0.5 : 0.0), dx));
+        const double z = __dadd_rn(oz, __dmul_rn((double)k + (c == 2 ? 0.5 : 0.0), dx));
+        unsigned long long key = 0;
+        for (int g = 0; g < n_regions; ++g) {
+            const int s = rstart[g], e = rstart[g + 1];
+            unsigned cnt = (unsigned)eval_program(nodes + s, e - s, x, y, z);
+            for (int q = 0; q < n_offs; ++q)
+                cnt += (unsigned)eval_program(nodes + s, e - s, __dadd_rn(x, offs[3 * q]),
+                                              __dadd_rn(y, offs[3 * q + 1]), __dadd_rn(z, offs[3 * q + 2]));
+            key |= (unsigned long long)cnt << (8 * g);
+        }
+        keys[c * kpitch + o] = key;
+        if (set) {
+            const unsigned peers = __match_any_sync(__activemask(), key);
+            if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) smooth_insert(set, cap, key, overflow);
+        }
+    }
+}
+
+cudaError_t launch_rasterize_counts(const sj_csg_node* d_nodes, const int* d_region_start, int n_regions,
+                                    int nx, int ny, int nz, double dx, const double* origin,
+                                    const double* d_offs, int n_offs, unsigned long long* d_keys,
+                                    long long key_pitch_elems, int px, unsigned long long* d_set,
+                                    unsigned cap, int* d_overflow, cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    k_rasterize_counts<<<blocks, 256, 0, s>>>(d_nodes, d_region_start, n_regions, nx, ny, nz, dx, origin[0],
+                                              origin[1], origin[2], d_offs, n_offs, d_keys, key_pitch_elems,
+                                              px, d_set, cap, d_overflow);
+    return cudaGetLastError();
+}
+
+// Replace each point's key by its index in the sorted list of distinct keys
+// (n_keys <= 256): the point's material class.
+__global__ void k_class_assign(const unsigned long long* __restrict__ keys, long long pitch, int nx, int ny,
+                               int nz, int px, const unsigned long long* __restrict__ sorted, int n_keys,
+                               uint8_t* __restrict__ cls) {
+    __shared__ unsigned long long sk[256];
+    for (int q = threadIdx.x; q < n_keys; q += blockDim.x) sk[q] = sorted[q];
+    __syncthreads();
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (t >= total) return;
+    const int i = (int)(t % nx);
+    const long long r = t / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    const long long o = ((long long)k * ny + j) * px + i;
+    for (int c = 0; c < 3; ++c) {
+        const unsigned long long key = keys[c * pitch + o];
+        int lo = 0, hi = n_keys - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sk[mid] < key)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        cls[c * pitch + o] = (uint8_t)lo;
+    }
+}
+
+cudaError_t launch_class_assign(const unsigned long long* d_keys, long long pitch, int nx, int ny, int nz,
+                                int px, const unsigned long long* d_sorted, int n_keys, uint8_t* d_cls,
+                                cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    k_class_assign<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(d_keys, pitch, nx, ny, nz, px, d_sorted,
+                                                                   n_keys, d_cls);
+    return cudaGetLastError();
+}
+
 // Mark every (class_x, class_y, class_z) triple present in a 2^24-bit set.
 __global__ void k_combo_mark(const uint8_t* __restrict__ cls, long long cpitch, int nx, int ny,
                              int nz, int px, uint32_t* __restrict__ bitmap) {
@@ -285,6 +404,10 @@ int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_
     }
     if (sc->n_regions < 0 || sc->n_regions > SJ_MAX_REGIONS || (sc->n_regions > 0 && !sc->regions)) {
         *msg = "scene n_regions must be in [0, 8]";
+        return SJ_E_INVALID;
+    }
+    if (sc->smooth_n != 0) {
+        *msg = "a smoothed scene has fill counts, not region masks (sj_rasterize_counts)";
         return SJ_E_INVALID;
     }
     int start[SJ_MAX_REGIONS + 1] = {0};

@@ -293,3 +293,24 @@ def rasterize(grid, scene):
     g = grid.to_c()
     _abi.check(lib, lib.sj_rasterize(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8))))
     return out
+
+
+def rasterize_counts(grid, scene):
+    """Per-region fill counts at the Ex/Ey/Ez points of `grid` under the scene's
+    stochastic smoothing ([3][n_regions][nz][ny][nx] uint8, 0 .. 8 smooth_n + 1)."""
+    from .spec import scene_to_c
+    lib = _abi.load_library()
+    sc, h = scene_to_c(scene)
+    out = np.zeros((3, len(scene.regions), grid.nz, grid.ny, grid.nx), dtype=np.uint8)
+    g = grid.to_c()
+    _abi.check(lib, lib.sj_rasterize_counts(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return out
+
+
+def smooth_points(smooth_n, smooth_rad):
+    """The smoothing offsets d_j of cgs_material_function ([8 smooth_n][3])."""
+    lib = _abi.load_library()
+    out = np.zeros((8 * smooth_n, 3), dtype=np.float64)
+    _abi.check(lib, lib.sj_smooth_points(smooth_n, smooth_rad, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                         out.size))
+    return out

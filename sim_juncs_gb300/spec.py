@@ -70,6 +70,10 @@ class Scene:
     regions: List[Region]
     ambient_eps: float = 1.0
     combine: int = _abi.EPS_SUM
+    # stochastic smoothing of cgs_material_function (src/disp.cpp:56-112,
+    # 264-283): 0 = off, the reference's default; smooth_rad in length units
+    smooth_n: int = 0
+    smooth_rad: float = 0.05
 
 
 @dataclass
@@ -201,6 +205,8 @@ class Instance:
             sc.ambient_eps = mat.ambient_eps
             sc.n_regions = len(regs)
             sc.combine = mat.combine
+            sc.smooth_n = int(mat.smooth_n)
+            sc.smooth_rad = float(mat.smooth_rad)
             sc.regions = h.keep(_array(_abi.RegionDesc, regs))
             h.keep(sc)
             m.scene = C.pointer(sc)

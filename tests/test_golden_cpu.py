@@ -102,12 +102,18 @@ def test_reference_inclusion_test_points():
     assert got.tolist() == tp["inside"]
 
 
+# the points of the reference's in_bound test (src/main_test.cpp:1629-1634);
+# the third differs from the in() test's (.65, .45, .41)
+IN_BOUND_POINTS = [(.45, .45, .45), (.45, .41, .6), (.65, .45, .45), (.71, .51, .51), (.55, .45, .45),
+                   (.55, .41, .85)]
+
+
 def test_in_bound_sum_values():
-    # src/main_test.cpp:1637-1642: in_bound = 3.5 at the first three points,
+    # src/main_test.cpp:1635-1640: in_bound = 3.5 at the first three points,
     # 1.0 at the others; in_bound (src/disp.cpp:264-283 with smooth_n = 0)
     # sums def + (eps_root - def) * in(r) over the roots
     e = G["files"]["tests/test.geom"]
-    pts = np.array(e["test_points"]["points"])
+    pts = np.array(IN_BOUND_POINTS)
     amb = 1.0
     val = np.zeros(len(pts))
     for r in e["roots"]:
