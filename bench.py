@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -101,7 +102,9 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # the raw samples: SJ_CLOCKS_DIR when set (to keep them), else the temp directory
+        base = os.environ.get("SJ_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(base, f"clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

@@ -4,7 +4,7 @@ differences and against the FP64 adjoint; print one JSON line.
     python -m sim_juncs_gb300.adjoint_check [--n 160] [--steps 4000]
         [--checkpoint 200] [--voxels 16] [--h 1e-3]
 
-Defaults are the c3 configuration (configs.adjoint_case): 160^3 at
+Defaults are the adjoint case (configs.adjoint_case): 160^3 at
 30 px/um, Au box pair, an 18 x 18 x 3 design region in the gap with
 eps ~ U[1, 4] (seed 1), |E(fcen)|^2 over a 5 x 5 gap patch, 4000 steps,
 checkpoints every 200 steps.  The finite differences use the FP64 forward

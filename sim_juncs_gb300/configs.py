@@ -3,15 +3,15 @@
 All lengths in um with um_scale = 1 (one meep length unit = 1 um), so
 meep frequencies are 1/wavelength(um) and times are um/c.
 
-  junction_c0   3.2 um cube at 20 px/um (64^3), 0.5 um PML, two Au boxes
+  junction      3.2 um cube at 20 px/um (64^3), 0.5 um PML, two Au boxes
                 1.0 x 0.5 x 0.1 um with a 0.2 um x-gap, current sheet 1.0 um
                 below the junction, fcen = 1/0.7, fwidth = 0.5, 2000 steps,
                 Courant 0.45 (see junction_instance)
-  bowtie_c1     512 x 512 x 384 at 40 px/um, 1.0 um PML, two Au triangular
+  bowtie        512 x 512 x 384 at 40 px/um, 1.0 um PML, two Au triangular
                 prisms (2.0 um tip-to-base, 60 deg apex, 0.05 um thick,
                 0.1 um tip gap) on a 1.0 um SiO2 slab (eps 2.13), fcen = 1/0.8,
                 32 x 32 Ez monitor plane + 50-frequency flux DFT
-  sweep_c2      96 junction instances: 32 each at 96^3 (30 px/um), 128^3
+  sweep         96 junction instances: 32 each at 96^3 (30 px/um), 128^3
                 (40 px/um), 192^3 (60 px/um), CEP ~ U[0, 2pi) and amplitude
                 log-uniform in [0.1, 10] from seed 0, Ez at 4 gap points
 Au: eps_inf = 1, Drude (omega_p = 7.3, gamma = 0.043 -> omega_0 = 1,
@@ -63,7 +63,7 @@ def gaussian_pulse(component, z_sheet, L, fcen, fwidth=0.5, cutoff=5.0, phase=0.
 def junction_instance(n=64, res=20.0, pml_um=0.5, phase=0.0, amplitude=1.0,
                       fcen=1 / 0.7, probe_components=("Ex", "Ez"), dft=True, save_span=20,
                       component=SHEET_COMPONENT):
-    """The Au box-pair junction of the c0 workload at grid n^3."""
+    """The Au box-pair junction (3.2 um cube, 0.2 um gap) at grid n^3."""
     dx = 1.0 / res
     L = n * dx
     c = L / 2
@@ -83,7 +83,7 @@ def junction_instance(n=64, res=20.0, pml_um=0.5, phase=0.0, amplitude=1.0,
 
 
 def bowtie_instance(nx=512, ny=512, nz=384, res=40.0, pml_um=1.0, n_freq=50, plane_n=32):
-    """The c1 bowtie: Au prisms on an SiO2 slab; FIRST-containing-root eps."""
+    """The 512 x 512 x 384 bowtie: Au prisms on an SiO2 slab; FIRST-containing-root eps."""
     dx = 1.0 / res
     Lx, Ly, Lz = nx * dx, ny * dx, nz * dx
     cx, cy, cz = Lx / 2, Ly / 2, Lz / 2
@@ -123,7 +123,7 @@ def bowtie_instance(nx=512, ny=512, nz=384, res=40.0, pml_um=1.0, n_freq=50, pla
 
 
 def sweep_instances(per_size=32, sizes=((96, 30.0), (128, 40.0), (192, 60.0)), seed=0):
-    """c2: CEP/amplitude sweep over uneven grids (same 3.2 um junction cell)."""
+    """The 96-instance CEP/amplitude sweep over uneven grids (same 3.2 um junction cell)."""
     rng = np.random.default_rng(seed)
     out = []
     for n, res in sizes:
@@ -136,7 +136,7 @@ def sweep_instances(per_size=32, sizes=((96, 30.0), (128, 40.0), (192, 60.0)), s
 
 
 def adjoint_case(n=160, res=30.0, seed=1, design_um=(0.6, 0.6, 0.1), patch=5):
-    """c3: the Au box-pair junction at n^3 (30 px/um: 160^3), a design region
+    """The adjoint case: the Au box-pair junction at n^3 (30 px/um: 160^3), a design region
     of design_um centred in the gap with eps ~ U[1, 4] from `seed`, and
     |E(fcen)|^2 summed over a patch x patch gap patch in the junction's
     mid plane.  Returns (instance, design, objective)."""
@@ -152,7 +152,7 @@ def adjoint_case(n=160, res=30.0, seed=1, design_um=(0.6, 0.6, 0.1), patch=5):
 
 
 def inverse_design_case(index, n=192, res=30.0, design_um=(0.8, 0.8, 0.1), patch=5):
-    """c4 design `index`: the Au box pair of c0 (Drude + Lorentz Au) on a
+    """Inverse-design instance `index`: the Au box pair of the junction (Drude + Lorentz Au) on a
     quartz substrate (eps_inf 2.1 plus one Lorentz term, f0 = 10, gamma = 0,
     sigma = 0.25) filling the cell below the boxes, at n^3 and `res` px/um
     (192^3, 30 px/um); a design_um region in the gap with eps ~ U[1, 4]

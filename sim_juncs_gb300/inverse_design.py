@@ -1,4 +1,4 @@
-"""Batched adjoint inverse design (the c4 loop); prints one JSON line.
+"""Batched adjoint inverse design (16 designs at 192^3); prints one JSON line.
 
     python -m sim_juncs_gb300.inverse_design [--designs 16] [--n 192]
         [--steps 5000] [--iters 50] [--checkpoint 200] [--lr 0.05]
