@@ -210,7 +210,7 @@ def run_ours(args):
     f, schedule, til, tune_ms = tuned_fields(insts, args.schedule, torch)
     if til is not None:
         cfg = dict(cfg, tile=f"32x{til[0]}", tma_ring=til[1], zseg=til[2], tiling="autotuned",
-                   autotune_ms_per_step=tune_ms)
+                   autotune_dry_ms_per_step=tune_ms)  # the tuner's launches load but do not store
     voxels = f.voxels()
     bytes_step = f.bytes_per_step()
 
