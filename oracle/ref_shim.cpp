@@ -275,4 +275,31 @@ int sjref_in(int h, int r, const double* pts, int64_t n, uint8_t* out) {
     return 0;
 }
 
+// A primitive built with the reference's own constructors, as its volume
+// test builds them (src/main_test.cpp:1448-1459), and its in() at n points.
+// kind 0: sphere(center, rad), a = {cx, cy, cz, rad}; kind 1: cylinder(center,
+// height, r1, r2), a = {cx, cy, cz, height, r1, r2}; kind 2: plane(p1, p2,
+// p3), a = the three points.
+static void primitive_eval(object& obj, const double* pts, int64_t n, uint8_t* out) {
+    for (int64_t q = 0; q < n; ++q) out[q] = (uint8_t)obj.in(vec3(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]));
+}
+
+int sjref_primitive_in(int kind, const double* a, const double* pts, int64_t n, uint8_t* out) {
+    vec3 c(a[0], a[1], a[2]);
+    if (kind == 0) {
+        sphere obj(c, a[3]);
+        primitive_eval(obj, pts, n, out);
+    } else if (kind == 1) {
+        cylinder obj(c, a[3], a[4], a[5]);
+        primitive_eval(obj, pts, n, out);
+    } else if (kind == 2) {
+        vec3 p2(a[3], a[4], a[5]), p3(a[6], a[7], a[8]);
+        plane obj(c, p2, p3);
+        primitive_eval(obj, pts, n, out);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
 }  // extern "C"

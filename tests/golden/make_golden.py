@@ -23,9 +23,15 @@ composite of it, the file records:
 fft_reference.json holds the reference's fft (src/data_utils.cpp:413-427) of
 seeded series of several lengths.
 
+volume_reference.json holds, for the sphere, cylinder and plane of the
+reference's volume test (src/main_test.cpp:1448-1489), the reference's own
+in() (the primitives built with its constructors) at the test's 10000 sample
+points: the Numerical Recipes LCG of src/main_test.hpp:17-33 from TEST_SEED,
+one point per four draws.
+
 The parser executes snapshot(...) statements (it draws an image file), so
-each file is parsed from a copy without them, written under the repository's
-git-ignored _work/ folder; snapshots do not change the geometry.  The
+each file is parsed from a copy without them, written to a temporary
+directory; snapshots do not change the geometry.  The
 junction files read their parameters from the context bound_geom builds
 (src/disp.cpp:28-50) and the --opts string scripts/run.sh passes; the values
 used are in OPTS below.
@@ -37,6 +43,7 @@ import json
 import os
 import re
 import sys
+import tempfile
 import zlib
 
 import numpy as np
@@ -49,7 +56,6 @@ from sim_juncs_gb300 import _abi  # noqa: E402
 
 LIB = os.path.join(REPO, "oracle", "_ref", "libsjref.so")
 OUT = os.path.join(HERE, "cgs_reference.json")
-SCRATCH = os.path.join(REPO, "_work", "golden_geom")
 GRID_N = 32
 # scripts/run.sh passes width, thick, inf_thick, wavelen and n_cycles
 OPTS = "width=0.1;thick=0.2;inf_thick=0;wavelen=0.7;n_cycles=0.5;snap_file=\"unused.pgm\""
@@ -161,9 +167,51 @@ def write_fft(lib):
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, fh)
 
 
+VOLUME_OUT = os.path.join(HERE, "volume_reference.json")
+TEST_SEED = 31415926
+TEST_N = 10000
+# the primitives of src/main_test.cpp:1452-1459 (kind, constructor arguments)
+VOLUME_PRIMITIVES = {"sphere": (0, [0.5, 0.5, 0.5, 0.5]),
+                     "cylinder": (1, [0.5, 0.5, 0.5, 0.5, 0.5, 0.5]),
+                     "plane": (2, [1.0, 1.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0])}
+
+
+def lcg_points(n=TEST_N, seed=TEST_SEED):
+    """The volume test's samples: state = lcg(lcg(seed)); per point three
+    draws for x, y, z and one more (src/main_test.cpp:1449-1469)."""
+    def lcg(v):
+        return (v * 1664525 + 1013904223) & 0xFFFFFFFF
+    state = lcg(lcg(seed))
+    pts = np.zeros((n, 3))
+    for q in range(n):
+        for a in range(3):
+            state = lcg(state)
+            pts[q, a] = state / 4294967295.0
+        state = lcg(state)
+    return pts
+
+
+def write_volumes(lib):
+    lib.sjref_primitive_in.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64,
+                                       C.POINTER(C.c_uint8)]
+    pts = np.ascontiguousarray(lcg_points())
+    prims = {}
+    for name, (kind, args) in VOLUME_PRIMITIVES.items():
+        a = (C.c_double * len(args))(*args)
+        out = np.zeros(len(pts), dtype=np.uint8)
+        rc = lib.sjref_primitive_in(kind, a, pts.ctypes.data_as(C.POINTER(C.c_double)), len(pts),
+                                    out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        assert rc == 0
+        prims[name] = {"kind": kind, "args": args, "inside_bits": pack_bits(out), "n_inside": int(out.sum())}
+    with open(VOLUME_OUT, "w") as fh:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": TEST_SEED, "n": TEST_N,
+                   "primitives": prims}, fh, indent=1)
+
+
 def main(ref_root):
     lib = load_lib()
-    os.makedirs(SCRATCH, exist_ok=True)
+    scratch = tempfile.TemporaryDirectory()
+    SCRATCH = scratch.name
     out = {"generator": "tests/golden/make_golden.py", "files": {}}
     for path in sorted(glob.glob(os.path.join(ref_root, "tests", "*.geom"))):
         name = os.path.relpath(path, ref_root)
@@ -197,6 +245,7 @@ def main(ref_root):
     with open(OUT, "w") as fh:
         json.dump(out, fh, indent=1)
     write_fft(lib)
+    write_volumes(lib)
     for name, e in out["files"].items():
         print(name, [(len(r["nodes"]), r["n_inside"], r["eps"], len(r["poles"])) for r in e["roots"]])
 

@@ -192,3 +192,42 @@ def test_reference_grid_rounding():
     assert g.nx == 65 and g.dt == pytest.approx(0.5 * g.dx)
     g, res = reference_grid(2.2, 0.5, 20.0, grid_num=64)   # an explicit grid number is kept
     assert g.nx == 64 and res == 20.0
+
+
+VOLUMES = os.path.join(os.path.dirname(__file__), "golden", "volume_reference.json")
+# src/main_test.cpp:1483-1485 (the sphere's 4/3 written 1.33333 there)
+VOLUME_KAT = {"sphere": 1.33333 * np.pi * 0.125, "plane": 5.0 / 6, "cylinder": np.pi * 0.125}
+
+
+def volume_primitives():
+    from sim_juncs_gb300.geometry import Cylinder, Plane, Sphere
+    # src/main_test.cpp:1452-1459
+    return {"sphere": Sphere((0.5, 0.5, 0.5), 0.5),
+            "cylinder": Cylinder((0.5, 0.5, 0.5), 0.5, 0.5, 0.5),
+            "plane": Plane((1.0, 1.0, 0.0), (0.0, 1.0, 1.0), (1.0, 0.0, 1.0))}
+
+
+def volume_points():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    with open(VOLUMES) as fh:
+        v = json.load(fh)
+    return v, mg.lcg_points(v["n"], v["seed"])
+
+
+def test_reference_volume_test_primitives():
+    # src/main_test.cpp:1448-1489: sampled volume fractions of a sphere, a
+    # cylinder and a plane within EPSILON = 0.01 of the exact volumes; the
+    # oracle answers the reference's own in() at every sample point
+    from sim_juncs_gb300.geometry import as_program
+    v, pts = volume_points()
+    assert pts.shape == (10000, 3) and 0.0 <= pts.min() and pts.max() <= 1.0
+    for name, obj in volume_primitives().items():
+        want = unpack(v["primitives"][name]["inside_bits"], len(pts))
+        got = oracle.csg_in(as_program(obj), pts)
+        np.testing.assert_array_equal(got, want)
+        frac = float(got.mean())
+        assert abs(VOLUME_KAT[name] - frac) / VOLUME_KAT[name] < 0.01, (name, frac)

@@ -39,3 +39,21 @@ def test_device_monitor_spectrum(lib):
         for m in range(mon.shape[0]):
             want = reference_spectrum(mon[m])
             assert float(np.max(np.abs(spec[m] - want))) <= 1e-12 * max(1e-300, float(np.max(np.abs(want))))
+
+
+def test_device_rasterizer_reference_volume_primitives(lib, oracle_lib):
+    # the sphere, cylinder and plane of src/main_test.cpp:1448-1489 rasterised
+    # on the unit cube: the device's masks equal the oracle's, and the filled
+    # fraction of each is within the test's EPSILON = 0.01 of its volume
+    from oracle.oracle import rasterize as oracle_rasterize
+    from sim_juncs_gb300.spec import Grid, Region, Scene
+    from test_golden_cpu import VOLUME_KAT, volume_primitives
+    n = 96
+    g = Grid(n, n, n, 1.0 / n, origin=(0.0, 0.0, 0.0))
+    prims = volume_primitives()
+    sc = Scene([Region(o, eps=2.0) for o in prims.values()])
+    masks = rasterize(g, sc)
+    np.testing.assert_array_equal(masks, oracle_rasterize(g, sc))
+    for r, name in enumerate(prims):
+        frac = float(((masks >> r) & 1).mean())
+        assert abs(frac - VOLUME_KAT[name]) / VOLUME_KAT[name] < 0.01, (name, frac)
