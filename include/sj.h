@@ -43,7 +43,9 @@
 extern "C" {
 #endif
 
-#define SJ_ABI_VERSION 1
+/* raised whenever a struct layout or a signature changes; 2: sj_scene_desc
+   gained smooth_n and smooth_rad */
+#define SJ_ABI_VERSION 2
 
 /* status codes */
 #define SJ_OK 0

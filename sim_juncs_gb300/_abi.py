@@ -164,6 +164,10 @@ class SJError(RuntimeError):
         self.code = code
 
 
+# SJ_ABI_VERSION of include/sj.h that these ctypes mirrors follow
+ABI_VERSION = 2
+
+
 def load_library(path=LIB_PATH):
     """Load the CUDA library; raises if it was not built (no CPU fallback)."""
     global _lib
@@ -178,6 +182,9 @@ def load_library(path=LIB_PATH):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.sj_abi_version() != ABI_VERSION:
+        raise ImportError(f"{path} implements ABI {lib.sj_abi_version()}, these bindings ABI {ABI_VERSION}: "
+                          "rebuild it with `python -m sim_juncs_gb300.build`")
     _lib = lib
     return lib
 

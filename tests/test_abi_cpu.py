@@ -36,7 +36,9 @@ def test_struct_layouts_match(lib):
 
 
 def test_abi_version(lib):
-    assert lib.sj_abi_version() == 1
+    text = open(HEADER).read()
+    declared = int(re.search(r"#define SJ_ABI_VERSION (\d+)", text).group(1))
+    assert lib.sj_abi_version() == declared == _abi.ABI_VERSION
 
 
 def test_source_helpers_run_on_host(lib):
