@@ -173,3 +173,32 @@ def test_oracle_classes_are_ranked_count_tuples():
     uniq = np.unique(key)
     assert len(uniq) > 4                               # fractional fills present
     np.testing.assert_array_equal(cls, np.searchsorted(uniq, key))
+
+
+def test_scene_smoothing_fields_reach_the_descriptor():
+    from sim_juncs_gb300.spec import scene_to_c
+    sc, h = scene_to_c(Scene([Region(Box((0, 0, 0), (1, 1, 1)), eps=2.0)], smooth_n=3, smooth_rad=0.2))
+    assert (sc.contents.smooth_n, sc.contents.smooth_rad) == (3, 0.2)
+    sc, h = scene_to_c(Scene([Region(Box((0, 0, 0), (1, 1, 1)), eps=2.0)]))
+    assert (sc.contents.smooth_n, sc.contents.smooth_rad) == (0, 0.05)    # off by default
+
+
+@pytest.mark.parametrize("change,why", [
+    (dict(smooth_n=32), "smooth_n"),
+    (dict(smooth_n=-1), "smooth_n"),
+    (dict(smooth_rad=0.0), "smooth_rad"),
+    (dict(smooth_rad=float("nan")), "smooth_rad"),
+    (dict(combine=_abi.EPS_FIRST), "SJ_EPS_SUM"),
+])
+def test_host_validates_smoothing_before_device_work(lib, change, why):
+    # the scene check runs on the host before any CUDA call, so it runs here
+    from sim_juncs_gb300.spec import scene_to_c
+    kw = dict(smooth_n=1, smooth_rad=0.05)
+    kw.update({k: v for k, v in change.items() if k != "combine"})
+    sc_py = Scene([Region(Box((0, 0, 0), (1, 1, 1)), eps=2.0)], combine=change.get("combine", _abi.EPS_SUM), **kw)
+    sc, h = scene_to_c(sc_py)
+    g = Grid(4, 4, 4, 0.25).to_c()
+    out = np.zeros(3 * 4 * 4 * 4, dtype=np.uint8)
+    rc = lib.sj_rasterize_counts(C.byref(g), sc, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    assert rc == _abi.SJ_E_INVALID
+    assert why in lib.sj_last_error(None).decode()
