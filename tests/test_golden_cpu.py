@@ -231,3 +231,33 @@ def test_reference_volume_test_primitives():
         np.testing.assert_array_equal(got, want)
         frac = float(got.mean())
         assert abs(VOLUME_KAT[name] - frac) / VOLUME_KAT[name] < 0.01, (name, frac)
+
+
+PHASES = os.path.join(os.path.dirname(__file__), "golden", "phases_reference.json")
+
+
+def test_phases_fixture_is_complete_and_regenerable():
+    # tests/golden/make_phases_golden.py ran the reference's own CEP/envelope
+    # extraction (scripts/phases.py, signal, as opt_pulse_full calls it) on
+    # seeded synthetic pulses and the oracle's junction monitors; each entry
+    # holds the reference's results or the exception it raised
+    import importlib.util
+    with open(PHASES) as fh:
+        ph = json.load(fh)
+    keys = {"f0", "phi", "t0_corr", "amp", "mu", "sig", "skew"}
+    kinds = {s["kind"] for s in ph["series"]}
+    assert kinds == {"synthetic", "junction64"}
+    for s in ph["series"]:
+        r = s["reference"]
+        assert len(s["t"]) == len(s["v"]) > 0
+        assert ("error" in r) or (keys <= set(r) and all(np.isfinite(r[k]).all() for k in keys))
+    assert sum("error" not in s["reference"] for s in ph["series"]) >= 16
+    spec = importlib.util.spec_from_file_location(
+        "make_phases_golden", os.path.join(os.path.dirname(__file__), "golden", "make_phases_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    synth = mg.synthetic_series(np.random.default_rng(ph["seed"]))
+    got = [s for s in ph["series"] if s["kind"] == "synthetic"]
+    assert len(synth) == len(got)
+    for a, b in zip(synth, got):
+        np.testing.assert_array_equal(np.array(a["v"]), np.array(b["v"]))
