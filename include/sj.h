@@ -68,8 +68,9 @@ enum { SJ_F64 = 0, SJ_F32 = 1 };
    instances with equal grids sharing launches); SPLIT the two-pass (H then
    E) schedule; TMA the single-pass kernel that stages tiles through a
    TMA/mbarrier shared-memory ring.  Default: FUSED for both precisions (the
-   fastest on GB300 for both); an instance with a design region (adjoint)
-   steps with SPLIT */
+   fastest on GB300 for both).  FUSED and SPLIT apply design regions
+   (adjoint); TMA does not, and a TMA sim moves to FUSED when a design
+   region is set */
 enum { SJ_SCHED_FUSED = 0, SJ_SCHED_SPLIT = 1, SJ_SCHED_TMA = 2 };
 
 #define SJ_MAX_POLES 8
@@ -372,8 +373,9 @@ int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out);
 
    Design region: a box of voxels whose eps_inf is given per voxel and
    applies at the voxel's Ex, Ey and Ez points (replacing the class table's
-   value there; polarisations of the voxel's class still apply).  An
-   instance with a design region steps with the split schedule.
+   value there; polarisations of the voxel's class still apply).  The
+   FUSED and SPLIT schedules apply it; a sim on the TMA schedule moves to
+   FUSED when a design region is set.
 
    Objective: F = sum over cells and over the E components in comp_mask of
    |D_c|^2 with D_c = sum_{n=0}^{N-1} dt E_c^n(cell) e^{+i 2 pi f n dt}, the
@@ -427,20 +429,25 @@ int sj_rasterize_counts(const sj_grid_desc* grid, const sj_scene_desc* scene, ui
 int sj_smooth_points(int32_t smooth_n, double smooth_rad, double* out, size_t cap);
 
 /* Allocation-free rasteriser (no counterpart in the reference).
-   For callers that cannot allocate device memory: code running while a
-   stream is being captured into a CUDA graph (cudaMalloc is not capturable),
-   or hosts whose device memory comes from their own pool.  Same result as
-   sj_rasterize, but the caller passes the output as a DEVICE buffer
-   d_out_masks[3][nz][ny][nx] and the work is queued on `stream` (a
-   cudaStream_t; NULL = the legacy default stream) without waiting for it.
-   The flattened CSG program is staged in one library-owned static device
-   array of SJ_RASTER_STATIC_NODES nodes in total, which every GPU that loads
-   the library holds until exit; larger scenes are rejected with SJ_E_RANGE.
-   The first call on a device looks up that array's address (once per
-   device) and must come before any stream capture.  All calls share the
-   array and it keeps the last call's program: calls that overlap on the GPU
-   (e.g. on two streams) race.  No cudaMalloc, cudaFree or other allocating
-   routine is called. */
+   For callers that cannot call cudaMalloc: hosts whose device memory is
+   handed out by a pool or caching allocator of their own (which may hold
+   nearly all of the GPU, so an allocation by this library would fail or
+   fragment it), and loops that must not stall on cudaMalloc/cudaFree, which
+   synchronise the device.  Same result as sj_rasterize, but the caller
+   passes the output as a DEVICE buffer d_out_masks[3][nz][ny][nx] and the
+   kernel is queued on `stream` (a cudaStream_t; NULL = the legacy default
+   stream).  The CSG program is copied from the caller's host arrays with
+   cudaMemcpyAsync; from pageable memory CUDA lets that copy start only after
+   the work already queued on `stream`, so the call may wait for it.  The
+   program is staged in one library-owned static device array of
+   SJ_RASTER_STATIC_NODES nodes in total (about 107 KB), which every GPU that
+   loads the library holds until exit; larger scenes are rejected with
+   SJ_E_RANGE.  The first call on a device (and the first after that device's
+   context is created anew) looks up the array's address; make that first
+   call before any stream capture.  All calls share the array and it keeps
+   the last call's program: calls that overlap on the GPU (e.g. on two
+   streams) race.  No cudaMalloc, cudaFree or other allocating routine is
+   called. */
 #define SJ_RASTER_STATIC_NODES 512
 int sj_rasterize_static(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* d_out_masks,
                         void* stream);

@@ -178,13 +178,16 @@ def load_library(path=LIB_PATH):
             f"{path} is missing: build it with `python -m sim_juncs_gb300.build` "
             "(the stepper has no CPU fallback)")
     lib = C.CDLL(path)
+    # the version first: a library of another ABI may lack later symbols
+    lib.sj_abi_version.restype = C.c_int
+    lib.sj_abi_version.argtypes = []
+    if lib.sj_abi_version() != ABI_VERSION:
+        raise ImportError(f"{path} implements ABI {lib.sj_abi_version()}, these bindings ABI {ABI_VERSION}: "
+                          "rebuild it with `python -m sim_juncs_gb300.build`")
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.sj_abi_version() != ABI_VERSION:
-        raise ImportError(f"{path} implements ABI {lib.sj_abi_version()}, these bindings ABI {ABI_VERSION}: "
-                          "rebuild it with `python -m sim_juncs_gb300.build`")
     _lib = lib
     return lib
 

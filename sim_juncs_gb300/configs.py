@@ -6,7 +6,7 @@ meep frequencies are 1/wavelength(um) and times are um/c.
   junction      3.2 um cube at 20 px/um (64^3), 0.5 um PML, two Au boxes
                 1.0 x 0.5 x 0.1 um with a 0.2 um x-gap, current sheet 1.0 um
                 below the junction, fcen = 1/0.7, fwidth = 0.5, 2000 steps,
-                Courant 0.45 (see junction_instance)
+                Courant 0.457 (stable_courant at 20 px/um)
   bowtie        512 x 512 x 384 at 40 px/um, 1.0 um PML, two Au triangular
                 prisms (2.0 um tip-to-base, 60 deg apex, 0.05 um thick,
                 0.1 um tip gap) on a 1.0 um SiO2 slab (eps 2.13), fcen = 1/0.8,
@@ -41,7 +41,7 @@ def stable_courant(res, omega_p=7.3, courant=0.5):
     Drude ADE stable: 12 S^2 + (2 pi omega_p S / res)^2 <= 4 (with a 5% margin).
 
     At 20 px/um the Au Drude term (omega_p = 7.3) violates this at S = 0.5
-    (the field grows ~1.5x per step), so the 64^3 junction runs at 0.45."""
+    (the field grows ~1.5x per step), so the 64^3 junction runs at 0.4573."""
     w = 2 * math.pi * omega_p / res
     smax = math.sqrt(4.0 / (12.0 + w * w)) * 0.95
     return min(courant, smax)

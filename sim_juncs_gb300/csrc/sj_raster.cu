@@ -76,8 +76,16 @@ __device__ int eval_program(const sj_csg_node* __restrict__ nodes, int n, double
     return (int)(stk & 1ull);
 }
 
-// One thread per voxel: masks for the Ex, Ey and Ez points.
-__global__ void k_rasterize(const sj_csg_node* __restrict__ nodes, const int* __restrict__ rstart,
+// Region start table carried by value in the kernel's parameters.
+struct RegionStarts {
+    int s[SJ_MAX_REGIONS + 1];
+    __device__ int operator[](int g) const { return s[g]; }
+};
+
+// One thread per voxel: masks for the Ex, Ey and Ez points.  Starts is a
+// device pointer to the region start table or a RegionStarts value.
+template <typename Starts>
+__global__ void k_rasterize(const sj_csg_node* __restrict__ nodes, const Starts rstart,
                             int n_regions, int nx, int ny, int nz, double dx, double ox, double oy,
                             double oz, uint8_t* __restrict__ masks, long long cpitch, int px) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -106,8 +114,9 @@ cudaError_t launch_rasterize(const sj_csg_node* d_nodes, const int* d_region_sta
                              uint8_t* d_masks, long long mask_pitch_elems, int px, cudaStream_t s) {
     const long long total = (long long)nx * ny * nz;
     const unsigned blocks = (unsigned)((total + 255) / 256);
-    k_rasterize<<<blocks, 256, 0, s>>>(d_nodes, d_region_start, n_regions, nx, ny, nz, dx,
-                                       origin[0], origin[1], origin[2], d_masks, mask_pitch_elems, px);
+    k_rasterize<const int*><<<blocks, 256, 0, s>>>(d_nodes, d_region_start, n_regions, nx, ny, nz, dx,
+                                                   origin[0], origin[1], origin[2], d_masks, mask_pitch_elems,
+                                                   px);
     return cudaGetLastError();
 }
 
@@ -353,18 +362,18 @@ cudaError_t launch_combo_hist(const uint8_t* d_combo, int nx, int ny, int nz, in
 // ---------------------------------------------------------------------------
 // Allocation-free rasteriser (sj_rasterize_static).
 //
-// The region start table and the concatenated CSG programs live in one
-// file-scope device array instead of cudaMalloc'd buffers.  Host code never
-// names the array directly: its device address comes from
-// cudaGetSymbolAddress, looked up once per device with that device current.
+// The concatenated CSG programs live in one file-scope device array instead
+// of cudaMalloc'd buffers; the region start table travels by value in the
+// kernel's parameters.  Host code never names the array directly: its device
+// address comes from cudaGetSymbolAddress, looked up with the device current
+// and cached per device together with the context it was taken in, so a
+// context torn down and created again (cudaDeviceReset) gets a fresh lookup.
+#include <cuda.h>
 #include <mutex>
 
 namespace sj {
 
-constexpr size_t RASTER_TABLE_BYTES = 64;  // int start[SJ_MAX_REGIONS + 1], padded
-constexpr size_t RASTER_SCRATCH_BYTES =
-    RASTER_TABLE_BYTES + (size_t)SJ_RASTER_STATIC_NODES * sizeof(sj_csg_node);
-static_assert((SJ_MAX_REGIONS + 1) * sizeof(int) <= RASTER_TABLE_BYTES, "region table too small");
+constexpr size_t RASTER_SCRATCH_BYTES = (size_t)SJ_RASTER_STATIC_NODES * sizeof(sj_csg_node);
 
 static __device__ __align__(256) unsigned char g_raster_scratch[RASTER_SCRATCH_BYTES];
 
@@ -372,6 +381,24 @@ namespace {
 constexpr int MAX_DEVICES = 64;
 std::mutex g_scratch_mu;
 unsigned char* g_scratch_ptr[MAX_DEVICES] = {};
+CUcontext g_scratch_ctx[MAX_DEVICES] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+
+// The driver's current context, through the runtime's entry-point table (the
+// library links only the CUDA runtime).
+cudaError_t current_context(CUcontext* out) {
+    static CtxGetCurrentFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    }
+    return fn(out) == CUDA_SUCCESS ? cudaSuccess : cudaErrorContextIsDestroyed;
+}
 
 // Device address of g_raster_scratch on the current device.
 cudaError_t raster_scratch(unsigned char** out) {
@@ -379,12 +406,20 @@ cudaError_t raster_scratch(unsigned char** out) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    CUcontext ctx = nullptr;
+    e = current_context(&ctx);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+        // no context yet (first CUDA call of this thread) or a new one: the
+        // lookup makes the device's primary context current if none is
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_raster_scratch);
         if (e != cudaSuccess) return e;
+        e = current_context(&ctx);
+        if (e != cudaSuccess) return e;
         g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return cudaSuccess;
@@ -410,7 +445,7 @@ int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_
         *msg = "a smoothed scene has fill counts, not region masks (sj_rasterize_counts)";
         return SJ_E_INVALID;
     }
-    int start[SJ_MAX_REGIONS + 1] = {0};
+    RegionStarts start = {};
     for (int r = 0; r < sc->n_regions; ++r) {
         const sj_region_desc& rg = sc->regions[r];
         if (rg.n_nodes < 1 || !rg.nodes) {
@@ -439,11 +474,11 @@ int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_
             *msg = "CSG program must leave exactly one value";
             return SJ_E_INVALID;
         }
-        if (start[r] + rg.n_nodes > SJ_RASTER_STATIC_NODES) {
+        if (start.s[r] + rg.n_nodes > SJ_RASTER_STATIC_NODES) {
             *msg = "scene has more CSG nodes than SJ_RASTER_STATIC_NODES (512)";
             return SJ_E_RANGE;
         }
-        start[r + 1] = start[r] + rg.n_nodes;
+        start.s[r + 1] = start.s[r] + rg.n_nodes;
     }
     unsigned char* base = nullptr;
     cudaError_t e = raster_scratch(&base);
@@ -452,16 +487,18 @@ int rasterize_static(const sj_grid_desc* g, const sj_scene_desc* sc, uint8_t* d_
         return SJ_E_CUDA;
     }
     // the program is overwritten in full by every call; nothing needs clearing
-    sj_csg_node* d_nodes = reinterpret_cast<sj_csg_node*>(base + RASTER_TABLE_BYTES);
-    int* d_start = reinterpret_cast<int*>(base);
-    e = cudaMemcpyAsync(d_start, start, sizeof(start), cudaMemcpyHostToDevice, s);
+    sj_csg_node* d_nodes = reinterpret_cast<sj_csg_node*>(base);
     for (int r = 0; r < sc->n_regions && e == cudaSuccess; ++r)
-        e = cudaMemcpyAsync(d_nodes + start[r], sc->regions[r].nodes,
+        e = cudaMemcpyAsync(d_nodes + start.s[r], sc->regions[r].nodes,
                             (size_t)sc->regions[r].n_nodes * sizeof(sj_csg_node), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
         const long long nv = (long long)g->nx * g->ny * g->nz;
-        e = launch_rasterize(d_nodes, d_start, sc->n_regions, g->nx, g->ny, g->nz, g->dx, g->origin, d_out,
-                             nv, g->nx, s);
+        const long long total = nv;
+        const unsigned blocks = (unsigned)((total + 255) / 256);
+        k_rasterize<RegionStarts><<<blocks, 256, 0, s>>>(d_nodes, start, sc->n_regions, g->nx, g->ny, g->nz,
+                                                         g->dx, g->origin[0], g->origin[1], g->origin[2], d_out,
+                                                         nv, g->nx);
+        e = cudaGetLastError();
     }
     if (e != cudaSuccess) {
         *msg = "CUDA call failed in sj_rasterize_static";

@@ -3,7 +3,7 @@
 Run where the reference checkout exists (argument: its root):
 
     make -C oracle ref
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference root>
 
 oracle/_ref/libsjref.so is the reference's src/cgs_read.cpp, cgs_data.cpp and
 cgs.cpp compiled unmodified, plus oracle/ref_shim.cpp.  For every .geom file
@@ -251,4 +251,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SJ_REFERENCE")
+    if not root:
+        sys.exit(f"usage: python {sys.argv[0]} <reference checkout root>  (or set SJ_REFERENCE)")
+    main(root)

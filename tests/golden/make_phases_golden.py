@@ -4,7 +4,7 @@ scripts/phases.py:735-758) returns for a set of monitor series.
 
 Run where the reference checkout exists (argument: its root):
 
-    python tests/golden/make_phases_golden.py /root/reference
+    python tests/golden/make_phases_golden.py <reference root>
 
 phases.py is imported unmodified.  Its module imports h5py and matplotlib
 for file input and plotting only; neither is installed here, so empty stand-in
@@ -114,4 +114,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SJ_REFERENCE")
+    if not root:
+        sys.exit(f"usage: python {sys.argv[0]} <reference checkout root>  (or set SJ_REFERENCE)")
+    main(root)

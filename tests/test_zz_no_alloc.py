@@ -1,9 +1,10 @@
 """The allocation-free rasteriser entry point, through the C ABI.
 
-sj_rasterize_static serves callers that cannot allocate device memory (code
-under CUDA-graph stream capture, or hosts that hand out device memory from
-their own pool): it writes into a device buffer the caller owns and stages
-the CSG program in a static device array.  Two calls in a row, on two
+sj_rasterize_static serves callers that cannot call cudaMalloc (hosts that
+hand out device memory from their own pool or caching allocator, loops that
+must not stall on the device-synchronising cudaMalloc/cudaFree): it writes
+into a device buffer the caller owns and stages the CSG program in a static
+device array.  Two calls in a row, on two
 different scenes, must each give exactly what the allocating sj_rasterize
 gives (integer masks: bit-exact).  This file is collected last on purpose.
 """
