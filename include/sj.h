@@ -363,8 +363,40 @@ int32_t sj_snapshots_pending(const sj_sim* sim, int32_t inst);
 int sj_write_field(sj_sim* sim, int32_t inst, int32_t component, const double* in, size_t n);
 /* per-component class map the stepper uses: out[3][nz][ny][nx] */
 int sj_read_class_map(sj_sim* sim, int32_t inst, uint8_t* out, size_t cap);
-/* largest |E| over the instance (divergence guard, src/disp.cpp:727-729) */
+/* largest |E| over the instance (a full-grid query; the step loop's own
+   guard is sj_set_divergence_guard) */
 int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out);
+
+/* Bounded device waits (no counterpart in the reference).  The TMA schedule's
+   kernels wait on mbarriers for their tile copies; a wait that does not end
+   within the limit gives up, the block waits (bounded by 100 ms) for the
+   copies it still has in flight and returns, and SJ_E_TIMEOUT is recorded:
+   sj_synchronize (and every call that synchronises) then returns it.  The
+   fields of that step are not valid.  ns = 0 restores the default of 100 ms
+   (a healthy copy takes microseconds); at most 10 s. */
+int sj_set_wait_limit(sj_sim* sim, int64_t ns);
+/* Test hook for the bounded waits: while on, the first tile block of every
+   TMA-schedule launch never fetches its second plane, so its wait on that
+   plane runs out after the limit and the launch records SJ_E_TIMEOUT.  No
+   other schedule is affected.  Off by default; for tests of a host's error
+   handling only. */
+int sj_set_test_stall(sj_sim* sim, int32_t on);
+
+/* Divergence guard of the time loop (src/disp.cpp:727-729, where
+   bound_geom::run prints every monitor sample whose real part exceeds 1000).
+   Every monitor sample is checked as it is taken, inside the probe kernels:
+   the first sample of the sim with |value| > bound, or that is NaN or
+   infinite, is recorded (step, instance, monitor, value) in host-mapped
+   memory.  From then on sj_step and sj_step_graph return SJ_E_DIVERGED
+   without queuing further steps, and sj_synchronize returns SJ_E_DIVERGED
+   once the queued steps are done; every read-back still works.  Steps queued
+   before the host saw the record still run.  bound = 0 switches the guard
+   off; default 1000 (the reference's threshold, applied to |value| rather
+   than to the real part only).  Setting a bound clears the record. */
+int sj_set_divergence_guard(sj_sim* sim, double bound);
+/* 1 and the record when the guard has tripped, 0 when not, -1 for NULL
+   (any output may be NULL; reads the record without synchronising) */
+int sj_divergence(const sj_sim* sim, int64_t* step, int32_t* inst, int32_t* monitor, double* value);
 
 /* ---------------------------------------------------------------- adjoint */
 /* Gradient of a gap-field objective with respect to per-voxel eps (the

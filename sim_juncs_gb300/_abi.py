@@ -146,6 +146,10 @@ SIGNATURES = {
     "sj_write_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),
     "sj_read_class_map": (C.c_int, [_P, C.c_int32, _U8, C.c_size_t]),
     "sj_max_abs_e": (C.c_int, [_P, C.c_int32, _D]),
+    "sj_set_divergence_guard": (C.c_int, [_P, C.c_double]),
+    "sj_set_wait_limit": (C.c_int, [_P, C.c_int64]),
+    "sj_set_test_stall": (C.c_int, [_P, C.c_int32]),
+    "sj_divergence": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D]),
     "sj_rasterize": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _U8]),
     "sj_rasterize_counts": (C.c_int, [C.POINTER(GridDesc), C.POINTER(SceneDesc), _U8]),
     "sj_smooth_points": (C.c_int, [C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_size_t]),

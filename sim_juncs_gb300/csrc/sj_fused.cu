@@ -25,8 +25,10 @@
 // A z segment starting at z0 > 0 first recomputes H of plane z0-1 (owned by
 // the previous segment), unstored.  Extra blocks after the stepping blocks
 // sample monitors and accumulate DFTs from buffer `cur`, which no block writes
-// during the launch.  Every wait on an mbarrier gives up after 100 ms and
-// records SJ_E_TIMEOUT in the device status instead of spinning forever.
+// during the launch.  Every wait on an mbarrier gives up after a limit (100 ms
+// unless sj_set_wait_limit sets another) and records SJ_E_TIMEOUT in the
+// device status instead of spinning forever; the block then waits, again
+// bounded (100 ms), for the copies it still has in flight and returns.
 #include <cuda.h>
 
 #include "sj_physics.cuh"
@@ -119,12 +121,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: false after WAIT_NS without completion.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait: false after limit_ns without completion.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = globaltimer();
     while (!mbar_try_wait(bar, parity)) {
-        if (globaltimer() - t0 > WAIT_NS) return false;
+        if (globaltimer() - t0 > limit_ns) return false;
     }
     return true;
 }
@@ -176,13 +178,7 @@ __device__ void probe_block(const InstDev<real>& I, long long chunk, long long n
         if (idx >= 0) v += I.probe_w[8 * p + m] * (double)F[idx];
     }
     const int ms = I.probe_mon[p];
-    if (ms >= 0 && (n % I.save_span) == 0) {
-        const long long s = n / I.save_span;
-        if (s < I.mon_cap)
-            I.mon[s * I.n_mon + ms] = v;
-        else
-            st->status = SJ_E_RANGE;
-    }
+    if (ms >= 0 && (n % I.save_span) == 0) monitor_store(I, n, ms, v, st);
     const int ds = I.probe_dft[p];
     if (ds >= 0) {
         double2* row = I.dft + (long long)ds * I.n_freq;
@@ -242,7 +238,7 @@ __device__ __forceinline__ real curl_c(const Cpml<real>& cp, real d1, real d2, c
 
 template <typename real, int TY, int NS>
 __device__ void step_block(const InstDev<real>& I, long long local, long long n, int cur, bool dry,
-                           DevState* st, unsigned char* smem) {
+                           DevState* st, unsigned char* smem, unsigned long long wait_ns, bool stall) {
     using L = Lay<real, TY, NS>;
     real* sRow = reinterpret_cast<real*>(smem + L::OFF_ROW);   // [2][TY+1][Hx, Hz][32]
     real* sCol = reinterpret_cast<real*>(smem + L::OFF_COL);   // [2][Hy, Hz][TY]
@@ -321,7 +317,12 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
         }
     };
     if (lead)
-        for (int p = kstart; p <= min(kend, kstart + NS - 1); ++p) issue(p, p - kstart);
+        for (int p = kstart; p <= min(kend, kstart + NS - 1); ++p) {
+            // test hook (sj_set_test_stall): the plane after the first is never
+            // fetched, so the first iteration's wait on it runs out
+            if (stall && p == kstart + 1) continue;
+            issue(p, p - kstart);
+        }
 
     const real S = I.S;
     const long long vol = I.vol;
@@ -432,8 +433,8 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
             }
         }
         if (do_h) {
-            if (q == 0) ok &= mbar_wait(smem_u32(&bars[sa]), pa);
-            ok &= mbar_wait(smem_u32(&bars[sb]), pb);
+            if (q == 0) ok &= mbar_wait(smem_u32(&bars[sa]), pa, wait_ns);
+            ok &= mbar_wait(smem_u32(&bars[sb]), pb, wait_ns);
             if (!ok) abort_flag = 1;
         }
         const real* E0 = reinterpret_cast<const real*>(smem + sa * L::SLOT);      // E of plane h
@@ -646,7 +647,8 @@ __device__ void step_block(const InstDev<real>& I, long long local, long long n,
         if (lead) {
             st->status = SJ_E_TIMEOUT;
             // bounded wait for every copy this block may still have in flight
-            for (int qq = 0; qq < NS; ++qq) mbar_wait(smem_u32(&bars[qq]), 0), mbar_wait(smem_u32(&bars[qq]), 1);
+            for (int qq = 0; qq < NS; ++qq)
+                mbar_wait(smem_u32(&bars[qq]), 0, WAIT_NS), mbar_wait(smem_u32(&bars[qq]), 1, WAIT_NS);
         }
         __syncthreads();
     }
@@ -682,7 +684,8 @@ k_fused(const InstDev<real>* __restrict__ insts, int n_inst, DevState* st, Fused
     }
     __syncthreads();
     if (stepping)
-        step_block<real, TY, NS>(sI, lb - pre[ii], n, cur, fl.dry != 0, st, smem);
+        step_block<real, TY, NS>(sI, lb - pre[ii], n, cur, fl.dry != 0, st, smem,
+                                 fl.wait_ns ? fl.wait_ns : WAIT_NS, fl.stall != 0 && b == 0);
     else if (!fl.dry)
         probe_block<real>(sI, lb - pre[ii], n, cur, st, reinterpret_cast<double2*>(smem));
     // the last block to finish advances the step and flips the buffers

@@ -157,6 +157,8 @@ struct sj_sim {
     // TMA schedule: tiling, tensor maps, block prefixes
     int f_ty = 8, f_zs = 64, f_ring = 3;
     bool fused_ready = false;
+    unsigned long long tma_wait_ns = 0;  // limit of a wait on a TMA copy (0 = the kernel's 100 ms)
+    int test_stall = 0;                  // sj_set_test_stall
     FusedLaunch fl{};
     void* d_fpre = nullptr;
     void* d_tmaps = nullptr;
@@ -183,6 +185,12 @@ struct sj_sim {
     // of older descriptors is captured again
     long long table_version = 0;
     long long graph_version = -1;
+    // divergence guard: bound, the device word electing the recorder and the
+    // host-mapped record (host and device addresses)
+    double guard_bound = 1000.0;
+    int* d_guard_flag = nullptr;
+    GuardRecord* h_guard = nullptr;
+    GuardRecord* d_guard = nullptr;
 
     ~sj_sim() {
         if (stream) cudaStreamSynchronize(stream);
@@ -196,6 +204,7 @@ struct sj_sim {
         if (ev_fork) cudaEventDestroy(ev_fork);
         drop_graphs();
         for (void* p : allocs) cudaFree(p);
+        if (h_guard) cudaFreeHost(h_guard);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
     // frees a snapshot ring (its copies must have finished)
@@ -948,6 +957,8 @@ void prepare_fused(sj_sim* sim) {
     fl.d_item_pre = reinterpret_cast<const long long*>(sim->d_fpre);
     fl.d_probe_pre = reinterpret_cast<const long long*>(sim->d_fpre) + (n + 1);
     fl.dry = 0;
+    fl.wait_ns = sim->tma_wait_ns;
+    fl.stall = sim->test_stall;
     upload_table<real>(sim);
     sim->fused_ready = true;
 }
@@ -1298,6 +1309,32 @@ int finish(sj_sim* sim, int code, const std::string& msg) {
         return finish(sim, SJ_E_INVALID, ex.what());               \
     }                                                              \
     return SJ_OK;
+
+// The divergence record as the host sees it (no synchronisation: the probe
+// that trips the guard writes it through host-mapped memory, flag last).
+bool diverged(const sj_sim* sim) {
+    return sim->h_guard && *reinterpret_cast<const volatile int*>(&sim->h_guard->flag) != 0;
+}
+
+void fail_if_diverged(const sj_sim* sim) {
+    if (!diverged(sim)) return;
+    const volatile GuardRecord* g = sim->h_guard;
+    char buf[200];
+    snprintf(buf, sizeof buf, "divergence at step %lld: instance %d monitor %d sampled %g (guard %g)",
+             (long long)g->step, g->inst, g->monitor, (double)g->value, sim->guard_bound);
+    fail(SJ_E_DIVERGED, buf);
+}
+
+template <typename real>
+void set_guard_t(sj_sim* sim, double bound) {
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    sim->guard_bound = bound;
+    for (auto& I : devv<real>(sim)) I.guard_bound = bound;
+    ck(cudaMemset(sim->d_guard_flag, 0, sizeof(int)), "guard reset");
+    memset(sim->h_guard, 0, sizeof(GuardRecord));
+    sim->drop_graphs();
+    upload_table<real>(sim);
+}
 
 int check_status(sj_sim* sim) {
     DevState st;
@@ -1679,7 +1716,13 @@ void create_t(sj_sim* sim, int n, const sj_instance_desc* insts) {
     auto& dv = devv<real>(sim);
     hv.resize(n);
     dv.resize(n);
-    for (int q = 0; q < n; ++q) build_instance<real>(sim, insts[q], hv[q], dv[q]);
+    for (int q = 0; q < n; ++q) {
+        build_instance<real>(sim, insts[q], hv[q], dv[q]);
+        dv[q].index = q;
+        dv[q].guard_bound = sim->guard_bound;
+        dv[q].guard_flag = sim->d_guard_flag;
+        dv[q].guard = sim->d_guard;
+    }
     sim->snaps.assign(n, Snapshots{});
     group_instances<real>(sim);
     upload_table<real>(sim);
@@ -1729,6 +1772,10 @@ int sj_batch_create(int32_t n, const sj_instance_desc* insts, int32_t precision,
         sim->own_stream = true;
         sim->d_state = (DevState*)sim->dalloc(sizeof(DevState));
         sim->d_scratch = (double*)sim->dalloc(64);
+        sim->d_guard_flag = (int*)sim->dalloc(sizeof(int));
+        ck(cudaHostAlloc((void**)&sim->h_guard, sizeof(GuardRecord), cudaHostAllocMapped), "guard record");
+        memset(sim->h_guard, 0, sizeof(GuardRecord));
+        ck(cudaHostGetDevicePointer((void**)&sim->d_guard, sim->h_guard, 0), "guard record address");
         if (precision == SJ_F64)
             create_t<double>(sim.get(), n, insts);
         else
@@ -1872,13 +1919,58 @@ int sj_synchronize(sj_sim* sim) {
     if (!sim) return SJ_E_INVALID;
     SJ_TRY(sim)
     check_status(sim);
+    fail_if_diverged(sim);
     SJ_CATCH(sim)
+}
+
+int sj_set_wait_limit(sj_sim* sim, int64_t ns) {
+    if (!sim) return SJ_E_INVALID;
+    if (ns < 0 || ns > 10000000000ll) return finish(sim, SJ_E_INVALID, "wait limit must be in [0, 10 s]");
+    SJ_TRY(sim)
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    sim->tma_wait_ns = (unsigned long long)ns;
+    sim->fl.wait_ns = sim->tma_wait_ns;
+    sim->drop_graphs();
+    SJ_CATCH(sim)
+}
+
+int sj_set_test_stall(sj_sim* sim, int32_t on) {
+    if (!sim) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    sim->test_stall = on ? 1 : 0;
+    sim->fl.stall = sim->test_stall;
+    sim->drop_graphs();
+    SJ_CATCH(sim)
+}
+
+int sj_set_divergence_guard(sj_sim* sim, double bound) {
+    if (!sim) return SJ_E_INVALID;
+    if (!(bound >= 0)) return finish(sim, SJ_E_INVALID, "guard bound must be >= 0 (0 = off)");
+    SJ_TRY(sim)
+    if (sim->precision == SJ_F64)
+        set_guard_t<double>(sim, bound);
+    else
+        set_guard_t<float>(sim, bound);
+    SJ_CATCH(sim)
+}
+
+int sj_divergence(const sj_sim* sim, int64_t* step, int32_t* inst, int32_t* monitor, double* value) {
+    if (!sim) return -1;
+    if (!diverged(sim)) return 0;
+    const volatile GuardRecord* g = sim->h_guard;
+    if (step) *step = g->step;
+    if (inst) *inst = g->inst;
+    if (monitor) *monitor = g->monitor;
+    if (value) *value = g->value;
+    return 1;
 }
 
 int sj_step(sj_sim* sim, int64_t n) {
     if (!sim) return SJ_E_INVALID;
     if (n < 0) return finish(sim, SJ_E_INVALID, "n_steps < 0");
     SJ_TRY(sim)
+    fail_if_diverged(sim);
     if (sim->precision == SJ_F64)
         do_steps<double>(sim, n);
     else
@@ -1890,6 +1982,7 @@ int sj_step_graph(sj_sim* sim, int64_t n, int32_t chunk) {
     if (!sim) return SJ_E_INVALID;
     if (n < 0) return finish(sim, SJ_E_INVALID, "n_steps < 0");
     SJ_TRY(sim)
+    fail_if_diverged(sim);
     if (sim->precision == SJ_F64)
         do_steps_graph<double>(sim, n, chunk);
     else

@@ -25,6 +25,18 @@ struct SrcDev {
     const double* tab;   // [steps]
 };
 
+// The first monitor sample that tripped the divergence guard, written by the
+// probe that found it into host-mapped pinned memory, so the host sees it
+// without synchronising the stream.  flag is written last.
+struct GuardRecord {
+    int flag;                   // 1 once a sample tripped the guard
+    int inst;                   // instance
+    int monitor;                // monitor column
+    int _pad;
+    long long step;             // the step the sample was taken before
+    double value;               // the sample
+};
+
 // Device-side view of one simulation instance.
 template <typename real>
 struct InstDev {
@@ -81,6 +93,13 @@ struct InstDev {
     // fused schedule: TMA descriptors and tiling
     const void* tmap;           // 31 CUtensorMap: E[b][c], H[b][c], combo, psiE[a][p], psiH[b][a][p]
     int f_ntx, f_nty, f_nzs, f_zs;  // tiles in x, y; z segments and their length
+
+    // divergence guard: a monitor sample with |v| > guard_bound, or not
+    // finite, is recorded once per sim (guard_bound = 0: off)
+    int index;                  // this instance's index in its sim
+    double guard_bound;
+    int* guard_flag;            // device word electing the one recorder
+    GuardRecord* guard;         // host-mapped record (device address)
 };
 
 // Step counter and status kept in device memory so that graph replays need
@@ -111,6 +130,8 @@ struct FusedLaunch {
     const long long* d_item_pre;   // [n_inst + 1] prefix of stepping blocks
     const long long* d_probe_pre;  // [n_inst + 1] prefix of probe blocks
     int dry;                    // 1 = time only: no step advance, no in-place stores
+    int stall;                  // test hook: block 0 never fetches its second plane
+    unsigned long long wait_ns; // limit of a wait on a TMA copy (0 = the default 100 ms)
 };
 template <typename real>
 cudaError_t launch_fused_step(const InstDev<real>* d_insts, int n_inst, DevState* st,

@@ -9,6 +9,33 @@
 
 namespace sj {
 
+// Store monitor sample v of monitor column ms taken before step n, and apply
+// the divergence guard (bound_geom::run flags samples above 1000,
+// src/disp.cpp:727-729): the first sample of the sim with |v| above the bound,
+// or not finite, is recorded in the host-mapped record, flag last.
+template <typename real>
+__device__ __forceinline__ void monitor_store(const InstDev<real>& I, long long n, int ms, double v,
+                                              DevState* st) {
+    const long long s = n / I.save_span;
+    if (s < I.mon_cap)
+        I.mon[s * I.n_mon + ms] = v;
+    else
+        st->status = SJ_E_RANGE;
+    const double b = I.guard_bound;
+    if (b > 0.0 && (!(fabs(v) <= b) || isinf(v)) && I.guard_flag) {
+        if (atomicCAS(I.guard_flag, 0, 1) == 0) {
+            GuardRecord* g = I.guard;
+            g->inst = I.index;
+            g->monitor = ms;
+            g->step = n;
+            g->value = v;
+            __threadfence_system();
+            *reinterpret_cast<volatile int*>(&g->flag) = 1;
+            __threadfence_system();
+        }
+    }
+}
+
 template <typename real>
 __device__ __forceinline__ int dim_of(const InstDev<real>& I, int a) {
     return a == 0 ? I.nx : (a == 1 ? I.ny : I.nz);

@@ -77,13 +77,7 @@ k_probe(const InstDev<real>* __restrict__ insts, DevState* st) {
         if (idx >= 0) v += I.probe_w[8 * p + m] * (double)F[idx];
     }
     const int ms = I.probe_mon[p];
-    if (ms >= 0 && (n % I.save_span) == 0) {
-        const long long s = n / I.save_span;
-        if (s < I.mon_cap)
-            I.mon[s * I.n_mon + ms] = v;
-        else
-            st->status = SJ_E_RANGE;
-    }
+    if (ms >= 0 && (n % I.save_span) == 0) monitor_store(I, n, ms, v, st);
     const int ds = I.probe_dft[p];
     if (ds >= 0) {
         double2* row = I.dft + (long long)ds * I.n_freq;

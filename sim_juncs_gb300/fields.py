@@ -283,6 +283,29 @@ class Fields:
         self._ck(self.lib.sj_max_abs_e(self.handle, inst, C.byref(v)))
         return v.value
 
+    # ------------------------------------------------------------ bounded waits
+    def set_wait_limit(self, ns):
+        """Limit of a TMA-schedule wait on a tile copy (0 = the default 100 ms)."""
+        self._ck(self.lib.sj_set_wait_limit(self.handle, int(ns)))
+
+    def set_test_stall(self, on):
+        """Test hook: the TMA schedule's first tile block skips a plane's
+        copy, so its wait runs out and SJ_E_TIMEOUT is reported."""
+        self._ck(self.lib.sj_set_test_stall(self.handle, 1 if on else 0))
+
+    # ------------------------------------------------------------ divergence guard
+    def set_divergence_guard(self, bound):
+        """Monitor samples with |value| > bound (or not finite) stop the loop
+        (src/disp.cpp:727-729 flags samples above 1000); 0 = off."""
+        self._ck(self.lib.sj_set_divergence_guard(self.handle, float(bound)))
+
+    def divergence(self):
+        """(step, instance, monitor, value) of the sample that tripped the
+        guard, or None."""
+        s, q, m, v = C.c_int64(), C.c_int32(), C.c_int32(), C.c_double()
+        r = self.lib.sj_divergence(self.handle, C.byref(s), C.byref(q), C.byref(m), C.byref(v))
+        return (s.value, q.value, m.value, v.value) if r == 1 else None
+
 
 def rasterize(grid, scene):
     """Region bitmasks at the Ex/Ey/Ez points of `grid` ([3][nz][ny][nx] uint8)."""
