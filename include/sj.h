@@ -382,6 +382,25 @@ int sj_set_wait_limit(sj_sim* sim, int64_t ns);
    handling only. */
 int sj_set_test_stall(sj_sim* sim, int32_t on);
 
+/* Discrete energy of instance inst in FP64 (the energy-conservation check;
+   the reference has no counterpart):
+     W = 1/2 dx^3 [ sum_E eps E^n E^n + sum_H H^{n-1/2} H^{n+1/2} ],
+   eps the stepper's own eps_inf (the design region's per-voxel value inside
+   it), H^{n+1/2} = H^{n-1/2} - S curl_fwd(E^n) formed on the fly.  For a
+   closed cavity (no CPML, no source) of non-dispersive material the leapfrog
+   conserves W exactly; its drift measures the arithmetic's rounding.
+   Polarisation energy is not included.  Synchronises the sim's stream. */
+int sj_energy(sj_sim* sim, int32_t inst, double* out);
+/* Flux spectrum through a surface sampled by DFT probes (the flux DFT of the
+   bowtie workload; meep's flux regions, which the reference does not use):
+     out[f] = dA * sum_p Re( E1_p(f) conj(H2_p(f)) - E2_p(f) conj(H1_p(f)) )
+   for every DFT frequency f; rows[p][4] are the DFT rows (the order of the
+   SJ_PROBE_DFT probes) of the tangential components E1, E2, H1, H2 of one
+   normal axis: x (Ey, Ez, Hy, Hz), y (Ez, Ex, Hz, Hx) or z (Ex, Ey, Hx, Hy),
+   each quadruple at one point.  FP64 on the device; cap >= n_freqs. */
+int sj_flux(sj_sim* sim, int32_t inst, int32_t n_points, const int32_t* rows, double dA, double* out,
+            size_t cap);
+
 /* Divergence guard of the time loop (src/disp.cpp:727-729, where
    bound_geom::run prints every monitor sample whose real part exceeds 1000).
    Every monitor sample is checked as it is taken, inside the probe kernels:

@@ -147,6 +147,8 @@ SIGNATURES = {
     "sj_read_class_map": (C.c_int, [_P, C.c_int32, _U8, C.c_size_t]),
     "sj_max_abs_e": (C.c_int, [_P, C.c_int32, _D]),
     "sj_set_divergence_guard": (C.c_int, [_P, C.c_double]),
+    "sj_energy": (C.c_int, [_P, C.c_int32, _D]),
+    "sj_flux": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_double, _D, C.c_size_t]),
     "sj_set_wait_limit": (C.c_int, [_P, C.c_int64]),
     "sj_set_test_stall": (C.c_int, [_P, C.c_int32]),
     "sj_divergence": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D]),

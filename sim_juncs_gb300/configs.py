@@ -122,6 +122,13 @@ def bowtie_instance(nx=512, ny=512, nz=384, res=40.0, pml_um=1.0, n_freq=50, pla
     return Instance(Grid(nx, ny, nz, dx, dt), scene, PML(pml_um), [src], probes, freqs, save_span=20)
 
 
+def bowtie_flux_rows(plane_n=32):
+    """DFT rows (Ex, Ey, Hx, Hy) of each point of bowtie_instance's plane, the
+    quadruples sj_flux takes for the z-normal flux through it."""
+    m = plane_n * plane_n
+    return [[p, m + p, 2 * m + p, 3 * m + p] for p in range(m)]
+
+
 def sweep_instances(per_size=32, sizes=((96, 30.0), (128, 40.0), (192, 60.0)), seed=0):
     """The 96-instance CEP/amplitude sweep over uneven grids (same 3.2 um junction cell)."""
     rng = np.random.default_rng(seed)

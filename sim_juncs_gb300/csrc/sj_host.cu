@@ -107,6 +107,7 @@ struct HostInst {
     std::vector<double*> d_tab;      // per source
     long long tab_cap = 0;
     std::vector<int> probe_flags;
+    std::vector<int> dft_comp;       // component of each DFT row
     int n_mon = 0, n_dft = 0, n_freq = 0;
     double* d_mon = nullptr;
     long long mon_cap = 0;
@@ -749,7 +750,10 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
         if (pd.component < 0 || pd.component > 5) fail(SJ_E_INVALID, "probe component out of range");
         pcomp[p] = pd.component;
         if (pd.flags & SJ_PROBE_MONITOR) pmon[p] = H.n_mon++;
-        if (pd.flags & SJ_PROBE_DFT) pdft[p] = H.n_dft++;
+        if (pd.flags & SJ_PROBE_DFT) {
+            pdft[p] = H.n_dft++;
+            H.dft_comp.push_back(pd.component);
+        }
         long long i0[3];
         double f[3];
         for (int a = 0; a < 3; ++a) {
@@ -2222,6 +2226,66 @@ int sj_max_abs_e(sj_sim* sim, int32_t inst, double* out) {
         ck(launch_max_abs_e<float>(sim->h32[inst], sim->cur, sim->d_scratch, sim->stream), "max");
     ck(cudaMemcpyAsync(out, sim->d_scratch, sizeof(double), cudaMemcpyDeviceToHost, sim->stream), "max read");
     ck(cudaStreamSynchronize(sim->stream), "sync");
+    SJ_CATCH(sim)
+}
+
+int sj_energy(sj_sim* sim, int32_t inst, double* out) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || !out) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    const int np = energy_partials();
+    double* part = (double*)sim->dalloc((size_t)(np + 1) * sizeof(double), false);
+    cudaError_t e;
+    if (sim->precision == SJ_F64) {
+        const double dx = sim->hi64[inst].dx;
+        e = launch_energy<double>(sim->h64[inst], sim->cur, 0.5 * dx * dx * dx, part, part + np, sim->stream);
+    } else {
+        const double dx = sim->hi32[inst].dx;
+        e = launch_energy<float>(sim->h32[inst], sim->cur, 0.5 * dx * dx * dx, part, part + np, sim->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, part + np, sizeof(double), cudaMemcpyDeviceToHost, sim->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sim->stream);
+    sim->dfree(part);
+    ck(e, "energy");
+    sim->d2h += (long long)sizeof(double);
+    SJ_CATCH(sim)
+}
+
+int sj_flux(sj_sim* sim, int32_t inst, int32_t n_points, const int32_t* rows, double dA, double* out, size_t cap) {
+    if (!sim || inst < 0 || inst >= sim->n_inst || n_points < 1 || !rows || !out) return SJ_E_INVALID;
+    SJ_TRY(sim)
+    const std::vector<int>& comp = sim->precision == SJ_F64 ? sim->hi64[inst].dft_comp : sim->hi32[inst].dft_comp;
+    const int n_freq = sim->precision == SJ_F64 ? sim->hi64[inst].n_freq : sim->hi32[inst].n_freq;
+    const double2* dft = sim->precision == SJ_F64 ? sim->h64[inst].dft : sim->h32[inst].dft;
+    if (n_freq < 1 || comp.empty()) fail(SJ_E_INVALID, "the instance has no DFT probes or frequencies");
+    if (cap < (size_t)n_freq) fail(SJ_E_RANGE, "output holds fewer than n_freqs values");
+    // (E1, E2, H1, H2) must be the tangential components of one normal axis
+    for (int p = 0; p < n_points; ++p) {
+        int c[4];
+        for (int m = 0; m < 4; ++m) {
+            const int r = rows[4 * p + m];
+            if (r < 0 || r >= (int)comp.size()) fail(SJ_E_RANGE, "DFT row out of range");
+            c[m] = comp[r];
+        }
+        bool ok = false;
+        for (int a = 0; a < 3; ++a) {
+            const int t1 = (a + 1) % 3, t2 = (a + 2) % 3;
+            ok |= c[0] == t1 && c[1] == t2 && c[2] == 3 + t1 && c[3] == 3 + t2;
+        }
+        if (!ok) fail(SJ_E_INVALID, "flux rows must be (E1, E2, H1, H2) tangential to one axis, in that order");
+    }
+    const size_t rb = (size_t)n_points * 4 * sizeof(int32_t);
+    char* buf = (char*)sim->dalloc(rb + (size_t)n_freq * sizeof(double), false);
+    cudaError_t e = cudaMemcpyAsync(buf, rows, rb, cudaMemcpyHostToDevice, sim->stream);
+    double* d_out = reinterpret_cast<double*>(buf + rb);  // rb = 16 n_points: 8-byte aligned
+    if (e == cudaSuccess)
+        e = launch_flux(dft, n_freq, reinterpret_cast<const int*>(buf), n_points, dA, d_out, sim->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d_out, (size_t)n_freq * sizeof(double), cudaMemcpyDeviceToHost, sim->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sim->stream);
+    sim->dfree(buf);
+    ck(e, "flux");
+    sim->h2d += (long long)rb;
+    sim->d2h += (long long)n_freq * (long long)sizeof(double);
     SJ_CATCH(sim)
 }
 

@@ -246,6 +246,15 @@ template <typename real>
 cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells, int n_cells, int comp_mask,
                              double freq, double2* d_D, long long n, bool sample, real* const* eb, cudaStream_t s);
 
+// Diagnostics (sj_diag.cu): the discrete energy (scale * sum, partial sums in
+// d_partial[energy_partials()]) and the flux spectrum of DFT-probe rows.
+int energy_partials();
+template <typename real>
+cudaError_t launch_energy(const InstDev<real>& h_inst, int cur, double scale, double* d_partial, double* d_out,
+                          cudaStream_t s);
+cudaError_t launch_flux(const double2* d_dft, int n_freq, const int* d_rows, int n_pts, double dA, double* d_out,
+                        cudaStream_t s);
+
 // Monitor spectra (sj_spectrum.cu): out[monitor][np][re, im] from the
 // monitor buffer mon[sample][n_mon] (n samples, np = 2^floor(log2 n)).
 cudaError_t launch_spectrum(const double* d_mon, int n_mon, long long n, long long np, double* d_out, cudaStream_t s);

@@ -283,6 +283,23 @@ class Fields:
         self._ck(self.lib.sj_max_abs_e(self.handle, inst, C.byref(v)))
         return v.value
 
+    # ------------------------------------------------------------ diagnostics
+    def energy(self, inst=0):
+        """Discrete leapfrog energy (FP64 sums; conserved by a closed,
+        source-free, non-dispersive cavity)."""
+        v = C.c_double()
+        self._ck(self.lib.sj_energy(self.handle, inst, C.byref(v)))
+        return v.value
+
+    def flux(self, rows, dA, inst=0):
+        """Flux spectrum through the points whose DFT rows (E1, E2, H1, H2)
+        are the rows of `rows` ([n_points][4]); one value per DFT frequency."""
+        r = np.ascontiguousarray(rows, dtype=np.int32).reshape(-1, 4)
+        out = np.zeros(len(self.instances[inst].freqs), dtype=np.float64)
+        self._ck(self.lib.sj_flux(self.handle, inst, len(r), r.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  float(dA), out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out
+
     # ------------------------------------------------------------ bounded waits
     def set_wait_limit(self, ns):
         """Limit of a TMA-schedule wait on a tile copy (0 = the default 100 ms)."""

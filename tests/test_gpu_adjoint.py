@@ -171,3 +171,66 @@ def test_design_on_one_member_splits_its_launch_group(lib):
         for c in range(6):
             np.testing.assert_array_equal(f.get_array(c, q), s.get_array(c), err_msg=f"instance {q} component {c}")
         s.close()
+
+
+def fd_case():
+    """48^3 junction at 15 px/um (the 3.2 um cell), pulse peaking at t = 2.5 so
+    that it has passed the gap within the run; a 6 x 6 x 2 design region in
+    the gap with eps ~ U[1, 4]; |E(fcen)|^2 of Ex and Ez over a 3 x 3 patch."""
+    from sim_juncs_gb300.configs import junction_instance
+    from sim_juncs_gb300.spec import Objective
+    inst = junction_instance(n=48, res=15.0, probe_components=("Ex",), dft=False)
+    for s in inst.sources:
+        shift = 0.5 * (s.start_time + s.end_time) - 2.5
+        s.start_time -= shift
+        s.end_time -= shift
+    c = 24
+    eps = np.random.default_rng(5).uniform(1.0, 4.0, size=(2, 6, 6))
+    des = Design((c - 3, c - 3, c - 1), eps)
+    cells = np.array([[c - 1 + a, c - 1 + b, c] for b in range(3) for a in range(3)])
+    return inst, des, Objective(cells, frequency=1 / 0.7, comps=(0, 2))
+
+
+FD_STEPS = 300
+
+
+@pytest.fixture(scope="module")
+def central_differences():
+    """(voxels, dF/deps by central differences, h = 1e-3) of the GPU FP64
+    forward path (sj_objective) at the two voxels of largest FP64 adjoint
+    gradient and two drawn from seed 7."""
+    inst, des, obj = fd_case()
+    f = Fields(inst, "f64")
+    f.set_design(des)
+    _, g = f.adjoint_gradient(obj, FD_STEPS, checkpoint_every=50)
+    order = np.argsort(-np.abs(g[0]).reshape(-1))
+    rnd = np.random.default_rng(7).choice(des.eps.size, size=2, replace=False)
+    flat = list(dict.fromkeys(list(order[:2]) + list(rnd)))
+    h = 1e-3
+    fd = []
+    for q in flat:
+        idx = np.unravel_index(q, des.eps.shape)
+        vals = []
+        for sgn in (1, -1):
+            e2 = des.eps.copy()
+            e2[idx] += sgn * h
+            f.set_design(Design(des.lo, e2))
+            vals.append(float(f.objective(obj, FD_STEPS)[0]))
+        fd.append((vals[0] - vals[1]) / (2 * h))
+    return flat, np.array(fd)
+
+
+@pytest.mark.parametrize("precision,schedule,tol", [("f64", "fused", 1e-5), ("f32", "fused", 1e-3),
+                                                     ("f32", "split", 1e-3)])
+def test_gpu_gradient_matches_central_differences(lib, central_differences, precision, schedule, tol):
+    flat, fd = central_differences
+    inst, des, obj = fd_case()
+    f = Fields(inst, precision, schedule)
+    f.set_design(des)
+    f.set_schedule(schedule)
+    _, g = f.adjoint_gradient(obj, FD_STEPS, checkpoint_every=50)
+    got = g[0].reshape(-1)[flat]
+    scale = float(np.max(np.abs(fd)))
+    assert scale > 0
+    err = float(np.max(np.abs(got - fd))) / scale
+    assert err <= tol, (precision, schedule, err)

@@ -134,3 +134,40 @@ def test_junction_gap_field_is_mirror_symmetric(oracle_lib):
     assert np.max(np.abs(m[0])) > 1e-3
     np.testing.assert_allclose(m[0], m[3], rtol=0, atol=1e-7 * np.max(np.abs(m[0])))
     np.testing.assert_allclose(m[1], m[2], rtol=0, atol=1e-7 * np.max(np.abs(m[0])))
+
+
+def cavity_energy(arrays_n, h_next, eps_maps, dx):
+    """W = 1/2 dx^3 [sum eps E^n E^n + sum H^{n-1/2} H^{n+1/2}] from the E^n,
+    H^{n-1/2} arrays and the H^{n+1/2} arrays one step later."""
+    w = sum((eps_maps[c] * arrays_n[c] * arrays_n[c]).sum() for c in range(3))
+    w += sum((arrays_n[3 + c] * h_next[c]).sum() for c in range(3))
+    return 0.5 * dx ** 3 * w
+
+
+def dielectric_cavity(n=20, seed=3):
+    """A closed cavity with a dielectric block (eps 2.5) in one corner and
+    random initial E."""
+    cm = np.zeros((3, n, n, n), dtype=np.uint8)
+    cm[:, 3:11, 5:14, 2:9] = 1
+    inst = Instance(Grid(n, n, n, 0.1), ClassMaterial(cm, [1.0, 2.5]), PML(0.0), save_span=1)
+    rng = np.random.default_rng(seed)
+    init = [rng.standard_normal((n, n, n)) for _ in range(3)]
+    eps = [np.where(cm[c] == 1, 2.5, 1.0) for c in range(3)]
+    return inst, init, eps
+
+
+def test_dielectric_cavity_conserves_the_energy_form(oracle_lib):
+    inst, init, eps = dielectric_cavity()
+    o = OracleFields(inst)
+    for c in range(3):
+        o.set_array(c, init[c])
+
+    def w_now():
+        a = [o.get_array(c) for c in range(6)]
+        o.step(1)
+        return cavity_energy(a, [o.get_array(c) for c in range(3, 6)], eps, inst.grid.dx)
+    w0 = w_now()
+    o.step(150)
+    w1 = w_now()
+    assert w0 > 0
+    assert abs(w1 - w0) / w0 < 1e-11
