@@ -44,8 +44,9 @@ extern "C" {
 #endif
 
 /* raised whenever a struct layout or a signature changes; 2: sj_scene_desc
-   gained smooth_n and smooth_rad */
-#define SJ_ABI_VERSION 2
+   gained smooth_n and smooth_rad; 3: the divergence guard, bounded-wait,
+   energy, flux and phase-extraction entry points and sj_phase_result */
+#define SJ_ABI_VERSION 3
 
 /* status codes */
 #define SJ_OK 0
@@ -255,7 +256,8 @@ typedef struct sj_sim sj_sim;
 /* ---------------------------------------------------------------- lifecycle */
 int sj_abi_version(void);
 /* sizeof of the descriptor structs above, in declaration order
-   (0 = sj_grid_desc ... 9 = sj_instance_desc); -1 for an unknown index */
+   (0 = sj_grid_desc ... 9 = sj_instance_desc, 10 = sj_design_desc,
+   11 = sj_objective_desc, 12 = sj_phase_result); -1 for an unknown index */
 int64_t sj_abi_struct_size(int32_t which);
 const char* sj_last_error(const sj_sim* sim);
 
@@ -502,6 +504,54 @@ int sj_smooth_points(int32_t smooth_n, double smooth_rad, double* out, size_t ca
 #define SJ_RASTER_STATIC_NODES 512
 int sj_rasterize_static(const sj_grid_desc* grid, const sj_scene_desc* scene, uint8_t* d_out_masks,
                         void* stream);
+
+/* ---------------------------------------------------------------- phase extraction */
+/* CEP and envelope of monitor series, on the device: the reference's analysis
+   class `signal` (scripts/phases.py:94-450) on the path its sweeps take,
+   signal(t, v, lowpass_inc) then get_envelope() and get_skewness(), one
+   thread block per series, FP64.  Per series: the t0 guess from the peaks of
+   v^2; V = 2 rfft(v rolled to t0); f0 = the trapezoid mean frequency of |V|
+   below twice its peak; sinc low-passes of strength lowpass_inc, 2
+   lowpass_inc, ... (at most 4) while f0 sits above half the band or |V| has
+   a prominent peak above 3 f0; the band where |V| > 0.1 |V(f0)|; a linear
+   regression of the unwrapped phase there (t0_corr = -slope / 2 pi, phi =
+   intercept wrapped to (-pi, pi]), recentred once when |t0_corr| > 2 / band
+   width; the envelope from |V| / (2 pi f) symmetrised about f0 with the
+   phase's odd-polynomial fit (solved as the linear least-squares problem the
+   reference's curve_fit converges to), and its moments.  Where the
+   reference raises, status says why and the fields computed before that
+   point are kept. */
+enum {
+    SJ_PHASE_OK = 0,
+    SJ_PHASE_NARROW_BAND = 1,   /* fewer than 5 band bins for the phase fit (curve_fit's TypeError):
+                                   f0, phi, t0_corr and the band are valid */
+    SJ_PHASE_EMPTY_BAND = 2,    /* zero-width band (the recentring test divides by it) */
+    SJ_PHASE_BAD_F0 = 3,        /* no finite central frequency inside the spectrum */
+    SJ_PHASE_BAD_T0 = 4         /* recentring moved t0 outside the series */
+};
+typedef struct {
+    double f0;                  /* central frequency (signal.f0) */
+    double phi;                 /* CEP: signal._phi_corr */
+    double t0_corr;             /* signal._t0_corr */
+    double t0;                  /* time of the largest |v| after filtering */
+    double amp[2];              /* the envelope at its maximum (numpy's complex argmax) */
+    double mu, sig, skew;       /* get_skewness: mean, width and skewness of |envelope| */
+    int32_t f0_ind;             /* f0's bin */
+    int32_t band_lo, band_hi;   /* the band [lo, hi) of the regression */
+    int32_t lowpass_steps;      /* low-pass strengths applied */
+    int32_t status;             /* SJ_PHASE_* */
+    int32_t _pad;
+} sj_phase_result;
+
+/* n_series series of n_samples (8 .. 4096) values each, v[series][sample],
+   sampled at t_pts[n_samples] (evenly spaced); results out[n_series].  Host
+   arrays; device memory is allocated for the call. */
+int sj_extract_phases(int32_t n_series, int32_t n_samples, const double* t_pts, const double* v,
+                      double lowpass_inc, sj_phase_result* out);
+/* Every monitor series of every instance of a sim, read where the stepper
+   keeps them (no host round trip), instance after instance, monitors in
+   probe order; sample k at time k save_span dt.  cap = entries of out. */
+int sj_extract_monitor_phases(sj_sim* sim, double lowpass_inc, sj_phase_result* out, size_t cap);
 
 /* ---------------------------------------------------------------- host helpers */
 /* gaussian_src_time_phase::dipole (src/disp.cpp:378-400) / meep's

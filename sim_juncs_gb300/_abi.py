@@ -96,8 +96,18 @@ class ObjectiveDesc(C.Structure):
                 ("_pad", C.c_int32), ("frequency", C.c_double)]
 
 
+class PhaseResult(C.Structure):
+    _fields_ = [("f0", C.c_double), ("phi", C.c_double), ("t0_corr", C.c_double), ("t0", C.c_double),
+                ("amp", C.c_double * 2), ("mu", C.c_double), ("sig", C.c_double), ("skew", C.c_double),
+                ("f0_ind", C.c_int32), ("band_lo", C.c_int32), ("band_hi", C.c_int32),
+                ("lowpass_steps", C.c_int32), ("status", C.c_int32), ("_pad", C.c_int32)]
+
+
+PHASE_OK, PHASE_NARROW_BAND, PHASE_EMPTY_BAND, PHASE_BAD_F0, PHASE_BAD_T0 = range(5)
+
 STRUCTS = {0: GridDesc, 1: Pole, 2: CsgNode, 3: RegionDesc, 4: SceneDesc, 5: MaterialDesc,
-           6: PmlDesc, 7: SourceDesc, 8: ProbeDesc, 9: InstanceDesc, 10: DesignDesc, 11: ObjectiveDesc}
+           6: PmlDesc, 7: SourceDesc, 8: ProbeDesc, 9: InstanceDesc, 10: DesignDesc, 11: ObjectiveDesc,
+           12: PhaseResult}
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -148,6 +158,8 @@ SIGNATURES = {
     "sj_max_abs_e": (C.c_int, [_P, C.c_int32, _D]),
     "sj_set_divergence_guard": (C.c_int, [_P, C.c_double]),
     "sj_energy": (C.c_int, [_P, C.c_int32, _D]),
+    "sj_extract_phases": (C.c_int, [C.c_int32, C.c_int32, _D, _D, C.c_double, C.POINTER(PhaseResult)]),
+    "sj_extract_monitor_phases": (C.c_int, [_P, C.c_double, C.POINTER(PhaseResult), C.c_size_t]),
     "sj_flux": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_double, _D, C.c_size_t]),
     "sj_set_wait_limit": (C.c_int, [_P, C.c_int64]),
     "sj_set_test_stall": (C.c_int, [_P, C.c_int32]),
@@ -171,7 +183,7 @@ class SJError(RuntimeError):
 
 
 # SJ_ABI_VERSION of include/sj.h that these ctypes mirrors follow
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 
 def load_library(path=LIB_PATH):

@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsj_gb300.so")
 OBJ = os.path.join(HERE, "_build")
 SOURCES = ["sj_host.cu", "sj_step.cu", "sj_lean.cu", "sj_fused.cu", "sj_raster.cu", "sj_adjoint.cu", "sj_spectrum.cu",
-           "sj_diag.cu"]
+           "sj_diag.cu", "sj_phases.cu"]
 HEADERS = ["sj_internal.h", "sj_physics.cuh", os.path.join("..", "..", "include", "sj.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

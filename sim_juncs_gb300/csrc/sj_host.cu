@@ -1753,6 +1753,7 @@ int64_t sj_abi_struct_size(int32_t which) {
         case 9: return sizeof(sj_instance_desc);
         case 10: return sizeof(sj_design_desc);
         case 11: return sizeof(sj_objective_desc);
+        case 12: return sizeof(sj_phase_result);
         default: return -1;
     }
 }
@@ -2370,6 +2371,95 @@ int sj_rasterize_static(const sj_grid_desc* grid, const sj_scene_desc* scene, ui
     const int rc = rasterize_static(grid, scene, d_out_masks, static_cast<cudaStream_t>(stream), &msg);
     if (rc != SJ_OK) return finish(nullptr, rc, msg);
     return SJ_OK;
+}
+
+int sj_extract_phases(int32_t n_series, int32_t n_samples, const double* t_pts, const double* v,
+                      double lowpass_inc, sj_phase_result* out) {
+    if (n_series < 0 || (n_series > 0 && (!t_pts || !v || !out)))
+        return finish(nullptr, SJ_E_INVALID, "NULL argument");
+    if (n_samples < 8 || n_samples > 4096) return finish(nullptr, SJ_E_INVALID, "n_samples must be in [8, 4096]");
+    if (!(lowpass_inc > 0)) return finish(nullptr, SJ_E_INVALID, "lowpass_inc must be > 0");
+    if (!(t_pts[1] - t_pts[0] > 0)) return finish(nullptr, SJ_E_INVALID, "t_pts must increase");
+    if (n_series == 0) return SJ_OK;
+    const size_t nv = (size_t)n_series * n_samples;
+    const size_t nw = (size_t)n_series * (size_t)phase_workspace(n_samples);
+    void* buf = nullptr;
+    const size_t bytes = (nv + n_samples + nw) * sizeof(double) + (size_t)n_series * sizeof(sj_phase_result);
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) return finish(nullptr, SJ_E_NOMEM, "cudaMalloc failed");
+    double* d_v = static_cast<double*>(buf);
+    double* d_t = d_v + nv;
+    double* d_w = d_t + n_samples;
+    sj_phase_result* d_out = reinterpret_cast<sj_phase_result*>(d_w + nw);
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_v, v, nv * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, t_pts, n_samples * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_phases(d_v, n_samples, 1, n_series, n_samples, d_t, lowpass_inc, d_w, d_out, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d_out, (size_t)n_series * sizeof(sj_phase_result), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (s) cudaStreamDestroy(s);
+    cudaFree(buf);
+    if (e != cudaSuccess) return finish(nullptr, SJ_E_CUDA, std::string("phase extraction: ") + cudaGetErrorString(e));
+    return SJ_OK;
+}
+
+int sj_extract_monitor_phases(sj_sim* sim, double lowpass_inc, sj_phase_result* out, size_t cap) {
+    if (!sim || !out) return SJ_E_INVALID;
+    if (!(lowpass_inc > 0)) return finish(sim, SJ_E_INVALID, "lowpass_inc must be > 0");
+    SJ_TRY(sim)
+    const int n = sim->n_inst;
+    std::vector<int> nmon(n), span(n);
+    std::vector<double> dt(n);
+    std::vector<const double*> mon(n);
+    for (int q = 0; q < n; ++q) {
+        if (sim->precision == SJ_F64)
+            nmon[q] = sim->hi64[q].n_mon, span[q] = sim->hi64[q].save_span, dt[q] = sim->hi64[q].dt,
+            mon[q] = sim->h64[q].mon;
+        else
+            nmon[q] = sim->hi32[q].n_mon, span[q] = sim->hi32[q].save_span, dt[q] = sim->hi32[q].dt,
+            mon[q] = sim->h32[q].mon;
+    }
+    size_t total = 0, wtotal = 0, ttotal = 0;
+    std::vector<int> ns(n);
+    for (int q = 0; q < n; ++q) {
+        ns[q] = (int)((sim->t + span[q] - 1) / span[q]);
+        if (nmon[q] == 0) continue;
+        if (ns[q] < 8 || ns[q] > 4096) fail(SJ_E_RANGE, "each series needs 8 .. 4096 monitor samples");
+        total += nmon[q];
+        wtotal += (size_t)nmon[q] * (size_t)phase_workspace(ns[q]);
+        ttotal += ns[q];
+    }
+    if (cap < total) fail(SJ_E_RANGE, "output holds fewer entries than the sim has monitors");
+    if (total == 0) return SJ_OK;
+    std::vector<double> ts;
+    ts.reserve(ttotal);
+    for (int q = 0; q < n; ++q)
+        if (nmon[q])
+            for (int k = 0; k < ns[q]; ++k) ts.push_back((double)k * (dt[q] * span[q]));
+    char* buf = (char*)sim->dalloc((ttotal + wtotal) * sizeof(double) + total * sizeof(sj_phase_result), false);
+    double* d_t = reinterpret_cast<double*>(buf);
+    double* d_w = d_t + ttotal;
+    sj_phase_result* d_out = reinterpret_cast<sj_phase_result*>(d_w + wtotal);
+    cudaError_t e = cudaMemcpyAsync(d_t, ts.data(), ttotal * sizeof(double), cudaMemcpyHostToDevice, sim->stream);
+    size_t so = 0, wo = 0, to = 0;
+    for (int q = 0; q < n && e == cudaSuccess; ++q) {
+        if (!nmon[q]) continue;
+        // mon[sample][n_mon]: series stride 1, sample stride n_mon
+        e = launch_phases(mon[q], 1, nmon[q], nmon[q], ns[q], d_t + to, lowpass_inc, d_w + wo, d_out + so,
+                          sim->stream);
+        so += nmon[q];
+        wo += (size_t)nmon[q] * (size_t)phase_workspace(ns[q]);
+        to += ns[q];
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d_out, total * sizeof(sj_phase_result), cudaMemcpyDeviceToHost, sim->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sim->stream);
+    sim->dfree(buf);
+    ck(e, "phase extraction");
+    sim->h2d += (long long)(ttotal * sizeof(double));
+    sim->d2h += (long long)(total * sizeof(sj_phase_result));
+    SJ_CATCH(sim)
 }
 
 int sj_source_dipole(const sj_source_desc* src, double t, double* re, double* im) {

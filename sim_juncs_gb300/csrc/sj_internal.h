@@ -255,6 +255,13 @@ cudaError_t launch_energy(const InstDev<real>& h_inst, int cur, double scale, do
 cudaError_t launch_flux(const double2* d_dft, int n_freq, const int* d_rows, int n_pts, double dA, double* d_out,
                         cudaStream_t s);
 
+// Phase extraction (sj_phases.cu): series q at d_v[q * s_series + k * s_sample],
+// k < N, times d_t[N]; per-series workspace phase_workspace(N) doubles.
+long long phase_workspace(int N);
+cudaError_t launch_phases(const double* d_v, long long s_series, long long s_sample, int n_series, int N,
+                          const double* d_t, double lowpass_inc, double* d_work, sj_phase_result* d_out,
+                          cudaStream_t s);
+
 // Monitor spectra (sj_spectrum.cu): out[monitor][np][re, im] from the
 // monitor buffer mon[sample][n_mon] (n samples, np = 2^floor(log2 n)).
 cudaError_t launch_spectrum(const double* d_mon, int n_mon, long long n, long long np, double* d_out, cudaStream_t s);

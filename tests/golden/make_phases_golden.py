@@ -17,10 +17,15 @@ records, a Gaussian-envelope carrier sampled every 20 steps with CEP drawn
 from [0, 2 pi) and amplitude log-uniform in [0.1, 10]; (2) the Ex and Ez gap
 monitors of the 64^3 junction run for 2000 steps on the FP64 oracle.  For each
 series the file holds the input and signal's f0, phi (_phi_corr), t0
-correction, the envelope peak opt_pulse_full stores as the amplitude, and the
-envelope's mean, width and skewness (get_skewness); or, where the reference
+correction, the envelope peak opt_pulse_full stores as the amplitude, the
+envelope's mean, width and skewness (get_skewness), f0's bin, the band of the
+phase fit, the low-pass strength reached and t0; or, where the reference
 raises (its phase fit needs at least five frequency bins in the band), the
-exception's type and message.
+exception's type and message.  "sensitivity" records how far the reference's
+own answers move when the input is perturbed by 1e-15 relative: the
+synthetic pulses, whose carrier sits near the sampling's Nyquist frequency,
+go through four low-pass steps that leave near-zero bins inside the band,
+and their phase fit then depends on rounding.
 """
 import contextlib
 import importlib.util
@@ -92,20 +97,45 @@ def extract(ph, t, v):
         env = s.get_envelope()
         k = int(np.argmax(env))
         mu, sig, skew, _ = s.get_skewness()
+        band = s._get_freq_fwhm()
     return {"f0": float(s.f0), "phi": float(s._phi_corr), "t0_corr": float(s._t0_corr),
             "amp": [float(env[k].real), float(env[k].imag)], "mu": float(mu), "sig": float(sig),
-            "skew": float(skew)}
+            "skew": float(skew), "f0_ind": int(s.f0_ind), "band": [int(band[0]), int(band[1])],
+            "lowpass_strength": float(s._low_stren), "t0": float(s.t0)}
+
+
+SENS_KEYS = ("f0", "phi", "t0_corr", "amp", "mu", "sig", "skew")
+
+
+def sensitivity(ph, t, v, ref, rng):
+    """How far the reference's own answers move when its input moves by
+    1e-15 relative (three seeded perturbations): near-zero spectral bins in
+    the band make the phase fit depend on rounding, and a port can match such
+    a series no closer than this."""
+    out = {k: 0.0 for k in SENS_KEYS}
+    v = np.asarray(v)
+    for _ in range(3):
+        try:
+            r = extract(ph, t, v * (1 + 1e-15 * rng.standard_normal(v.size)))
+        except Exception:
+            return {k: float("inf") for k in SENS_KEYS}
+        for k in SENS_KEYS:
+            out[k] = max(out[k], float(np.max(np.abs(np.asarray(r[k]) - np.asarray(ref[k])))))
+    return out
 
 
 def main(ref_root):
     ph = load_phases(ref_root)
     rng = np.random.default_rng(SEED)
     series = synthetic_series(rng) + junction_series()
+    prng = np.random.default_rng(SEED + 1)
     for s in series:
         try:
             s["reference"] = extract(ph, s["t"], s["v"])
         except Exception as e:  # the reference raises on some series; that is recorded too
             s["reference"] = {"error": type(e).__name__, "message": str(e)}
+        else:
+            s["sensitivity"] = sensitivity(ph, s["t"], s["v"], s["reference"], prng)
     with open(OUT, "w") as fh:
         json.dump({"generator": "tests/golden/make_phases_golden.py", "seed": SEED, "series": series}, fh)
     for s in series:
