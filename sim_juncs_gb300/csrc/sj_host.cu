@@ -527,23 +527,24 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
 
     // ---- combos: distinct (class_x, class_y, class_z) triples
     {
-        uint32_t* d_bitmap = (uint32_t*)sim->dalloc((1u << 24) / 8);
+        // one bit per (cx, cy, cz) triple present, compacted on the device to
+        // at most 257 keys (count first), so only those cross to the host
+        constexpr int KCAP = 257;
+        const int n_words = (1 << 24) / 32;
+        uint32_t* d_bitmap = (uint32_t*)sim->dalloc((size_t)n_words * 4 + (KCAP + 1) * 4);
+        uint32_t* d_found = d_bitmap + n_words;  // [0] = count, then the keys
         ck(launch_combo_mark(d_cls, cpitch, nx, ny, nz, px, d_bitmap, st), "combo mark");
-        std::vector<uint32_t> bitmap((1u << 24) / 32);
-        ck(cudaMemcpyAsync(bitmap.data(), d_bitmap, bitmap.size() * 4, cudaMemcpyDeviceToHost, st), "bitmap");
-        sim->d2h += (long long)bitmap.size() * 4;
+        ck(launch_combo_compact(d_bitmap, n_words, d_found + 1, KCAP, reinterpret_cast<int*>(d_found), st),
+           "combo compact");
+        std::vector<uint32_t> found(KCAP + 1);
+        ck(cudaMemcpyAsync(found.data(), d_found, found.size() * 4, cudaMemcpyDeviceToHost, st), "combo keys");
+        sim->d2h += (long long)found.size() * 4;
         ck(cudaStreamSynchronize(st), "combo sync");
-        H.keys.clear();
-        for (uint32_t w = 0; w < bitmap.size(); ++w) {
-            uint32_t bits = bitmap[w];
-            while (bits) {
-                const int b = __builtin_ctz(bits);
-                bits &= bits - 1;
-                H.keys.push_back(w * 32 + b);
-            }
-        }
         sim->dfree(d_bitmap);
-        if (H.keys.size() > 256) fail(SJ_E_INVALID, "more than 256 distinct material combos");
+        const int n_found = (int)found[0];
+        if (n_found > 256) fail(SJ_E_INVALID, "more than 256 distinct material combos");
+        H.keys.assign(found.begin() + 1, found.begin() + 1 + n_found);
+        std::sort(H.keys.begin(), H.keys.end());
         for (uint32_t k : H.keys)
             for (int c = 0; c < 3; ++c)
                 if ((int)((k >> (8 * c)) & 255) >= n_classes)

@@ -284,6 +284,8 @@ cudaError_t launch_class_assign(const unsigned long long* d_keys, long long pitc
                                 cudaStream_t s);
 cudaError_t launch_combo_mark(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
                               int px, uint32_t* d_bitmap, cudaStream_t s);
+cudaError_t launch_combo_compact(const uint32_t* d_bitmap, int n_words, uint32_t* d_keys, int cap, int* d_count,
+                                 cudaStream_t s);
 cudaError_t launch_combo_assign(const uint8_t* d_cls, long long cpitch, int nx, int ny, int nz,
                                 int px, const uint32_t* d_keys, int n_keys, uint8_t* d_combo,
                                 cudaStream_t s);

@@ -264,6 +264,27 @@ cudaError_t launch_combo_mark(const uint8_t* d_cls, long long cpitch, int nx, in
     return cudaGetLastError();
 }
 
+// The set bits of the triple bitmap as a key list (unordered; the host sorts
+// the at most cap it reads back).  *count gets the number of set bits.
+__global__ void k_combo_compact(const uint32_t* __restrict__ bitmap, int n_words, uint32_t* __restrict__ keys,
+                                int cap, int* __restrict__ count) {
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n_words; w += gridDim.x * blockDim.x) {
+        uint32_t bits = bitmap[w];
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int slot = atomicAdd(count, 1);
+            if (slot < cap) keys[slot] = (uint32_t)w * 32u + (uint32_t)b;
+        }
+    }
+}
+
+cudaError_t launch_combo_compact(const uint32_t* d_bitmap, int n_words, uint32_t* d_keys, int cap, int* d_count,
+                                 cudaStream_t s) {
+    k_combo_compact<<<608, 256, 0, s>>>(d_bitmap, n_words, d_keys, cap, d_count);
+    return cudaGetLastError();
+}
+
 // Replace each voxel's triple by its index in the sorted key list.
 __global__ void k_combo_assign(const uint8_t* __restrict__ cls, long long cpitch, int nx, int ny,
                                int nz, int px, const uint32_t* __restrict__ keys, int n_keys,
