@@ -2382,14 +2382,16 @@ int sj_extract_phases(int32_t n_series, int32_t n_samples, const double* t_pts, 
     if (!(lowpass_inc > 0)) return finish(nullptr, SJ_E_INVALID, "lowpass_inc must be > 0");
     if (!(t_pts[1] - t_pts[0] > 0)) return finish(nullptr, SJ_E_INVALID, "t_pts must increase");
     if (n_series == 0) return SJ_OK;
-    const size_t nv = (size_t)n_series * n_samples;
+    // every region starts on a 16-double boundary (the workspace holds double2 arrays)
+    auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    const size_t nv = al((size_t)n_series * n_samples);
     const size_t nw = (size_t)n_series * (size_t)phase_workspace(n_samples);
     void* buf = nullptr;
-    const size_t bytes = (nv + n_samples + nw) * sizeof(double) + (size_t)n_series * sizeof(sj_phase_result);
+    const size_t bytes = (nv + al(n_samples) + nw) * sizeof(double) + (size_t)n_series * sizeof(sj_phase_result);
     if (cudaMalloc(&buf, bytes) != cudaSuccess) return finish(nullptr, SJ_E_NOMEM, "cudaMalloc failed");
     double* d_v = static_cast<double*>(buf);
     double* d_t = d_v + nv;
-    double* d_w = d_t + n_samples;
+    double* d_w = d_t + al(n_samples);
     sj_phase_result* d_out = reinterpret_cast<sj_phase_result*>(d_w + nw);
     cudaStream_t s = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
@@ -2438,9 +2440,10 @@ int sj_extract_monitor_phases(sj_sim* sim, double lowpass_inc, sj_phase_result* 
     for (int q = 0; q < n; ++q)
         if (nmon[q])
             for (int k = 0; k < ns[q]; ++k) ts.push_back((double)k * (dt[q] * span[q]));
-    char* buf = (char*)sim->dalloc((ttotal + wtotal) * sizeof(double) + total * sizeof(sj_phase_result), false);
+    const size_t tpad = (ttotal + 15) & ~(size_t)15;  // the workspace after it starts on a 16-double boundary
+    char* buf = (char*)sim->dalloc((tpad + wtotal) * sizeof(double) + total * sizeof(sj_phase_result), false);
     double* d_t = reinterpret_cast<double*>(buf);
-    double* d_w = d_t + ttotal;
+    double* d_w = d_t + tpad;
     sj_phase_result* d_out = reinterpret_cast<sj_phase_result*>(d_w + wtotal);
     cudaError_t e = cudaMemcpyAsync(d_t, ts.data(), ttotal * sizeof(double), cudaMemcpyHostToDevice, sim->stream);
     size_t so = 0, wo = 0, to = 0;

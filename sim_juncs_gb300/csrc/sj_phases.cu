@@ -308,11 +308,30 @@ __device__ void odd_poly_fit(const double* ang, int lo, int n, double df, double
 
 }  // namespace
 
-// Per-series workspace, in doubles, for N samples (M = N / 2 + 1 bins).
-long long phase_workspace(int N) {
-    const long long M = N / 2 + 1;
-    return 3LL * N + 6 * M + 6LL * N + 5LL * 256 + 256;
-}
+// Per-series workspace layout, in doubles, for N samples (M = N / 2 + 1
+// bins): every array starts on a 16-double (128-byte) boundary, so the
+// double2 arrays are 16-byte aligned whatever N is.
+struct PhaseLay {
+    long long v0, v, vabs2, vf0, vf, mags, ef, vef, env, envt, scratch, total;
+    __host__ __device__ explicit PhaseLay(int N) {
+        const long long M = N / 2 + 1;
+        auto al = [](long long x) { return (x + 15) & ~15LL; };
+        v0 = 0;
+        v = v0 + al(N);
+        vabs2 = v + al(N);
+        vf0 = vabs2 + al(N);
+        vf = vf0 + al(2 * M);
+        mags = vf + al(2 * M);
+        ef = mags + al(M);
+        vef = ef + al(N);
+        env = vef + al(N);
+        envt = env + al(2LL * N);
+        scratch = envt + al(2LL * N);
+        total = scratch + al(5 * 256 + 256);
+    }
+};
+
+long long phase_workspace(int N) { return PhaseLay(N).total; }
 
 // series q: v[q * s_series + k * s_sample], k < N; t[k] the sample times.
 __global__ void __launch_bounds__(PH_THREADS)
@@ -321,18 +340,19 @@ k_phases(const double* __restrict__ vin, long long s_series, long long s_sample,
     __shared__ Ctl C;
     const int q = blockIdx.x;
     const int M = N / 2 + 1;
-    double* w = work + (long long)q * wstride;
-    double* v0 = w;                     // original series
-    double* v = v0 + N;                 // v_pts
-    double* vabs2 = v + N;              // v^2 (find_peaks input)
-    double2* vf0 = reinterpret_cast<double2*>(vabs2 + N);  // [M]
-    double2* vf = vf0 + M;              // [M]
-    double* mags = reinterpret_cast<double*>(vf + M);      // [M]
-    double* ef = mags + M;              // [N]
-    double* vef = ef + N;               // [N]
-    double2* env = reinterpret_cast<double2*>(vef + N);    // [N] Fourier envelope, then envelope
-    double2* envt = env + N;            // [N]... uses 2N doubles
-    double* scratch = reinterpret_cast<double*>(envt + N); // 5 * 256 + 256
+    const PhaseLay lay(N);
+    double* w = work + (long long)q * wstride;  // wstride: a multiple of 16 doubles
+    double* v0 = w + lay.v0;                    // original series
+    double* v = w + lay.v;                      // v_pts
+    double* vabs2 = w + lay.vabs2;              // v^2 (find_peaks input)
+    double2* vf0 = reinterpret_cast<double2*>(w + lay.vf0);   // [M]
+    double2* vf = reinterpret_cast<double2*>(w + lay.vf);     // [M]
+    double* mags = w + lay.mags;                // [M]
+    double* ef = w + lay.ef;                    // [N]
+    double* vef = w + lay.vef;                  // [N]
+    double2* env = reinterpret_cast<double2*>(w + lay.env);   // [N] Fourier envelope
+    double2* envt = reinterpret_cast<double2*>(w + lay.envt); // [N] envelope
+    double* scratch = w + lay.scratch;          // 5 * 256 + 256
     const double dt = t[1] - t[0];
     const double df = 1.0 / ((double)N * dt);  // rfftfreq spacing
 
