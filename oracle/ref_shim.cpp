@@ -5,11 +5,11 @@
 //
 // It does three things a maintainer wiring bound_geom to include/sj.h does:
 //   * parse a .geom file with the reference's scene (src/cgs.cpp:577);
-//   * flatten each root composite_object into sj_csg_node postfix programs,
-//     the walk of the integration guide, reading each node's trans_mat,
-//     invert and the cylinder's squared radii (r1_sq, r2_sq), which the
-//     reference keeps non-public; the guide asks for one-line accessors,
-//     and here the standard explicit-instantiation idiom reads them;
+//   * flatten each root composite_object into sj_csg_node postfix programs
+//     with the integration guide's own code (copied
+//     verbatim into _ref/guide_flatten.inc at build time), compiled against
+//     the reference's cgs.hpp with the four accessors the guide asks for
+//     (trans_mat, invert, the cylinder's r1_sq and r2_sq; oracle/guide_build.py);
 //   * restate parse_susceptibilities (src/disp.cpp:418-454), which lives in
 //     meep-dependent code, on the root's "susceptibilities" metadata.
 // It also exposes composite_object::in (src/cgs.cpp:431-456) itself and the
@@ -23,94 +23,18 @@
 #include "cgs.hpp"
 #include "cgs_read.hpp"
 #include "data_utils.hpp"
-#include "../include/sj.h"
+#include "sj.h"
 
 namespace {
 
-// Reads a non-public data member through a pointer-to-member obtained by
-// explicit template instantiation (which may name any member).
-template <typename Tag, typename Tag::type M>
-struct Reader {
-    friend typename Tag::type member_of(Tag) { return M; }
-};
-struct ObjTrans { typedef mat3x3 object::*type; friend type member_of(ObjTrans); };
-struct ObjInvert { typedef int object::*type; friend type member_of(ObjInvert); };
-struct CylR1 { typedef double cylinder::*type; friend type member_of(CylR1); };
-struct CylR2 { typedef double cylinder::*type; friend type member_of(CylR2); };
-template struct Reader<ObjTrans, &object::trans_mat>;
-template struct Reader<ObjInvert, &object::invert>;
-template struct Reader<CylR1, &cylinder::r1_sq>;
-template struct Reader<CylR2, &cylinder::r2_sq>;
-
-const mat3x3& trans_of(const object* o) { return o->*member_of(ObjTrans()); }
-int invert_of(const object* o) { return o->*member_of(ObjInvert()); }
-
 std::vector<scene*> g_scenes;
 
-void mat_copy(double* d, const mat3x3& m) {
-    for (int q = 0; q < 9; ++q) d[q] = m.el[q];
-}
+}  // namespace
 
-// acc = product of the ancestors' trans_mat (identity at the root)
-void flatten(const object* o, object_type t, const mat3x3& acc, std::vector<sj_csg_node>& out) {
-    sj_csg_node n;
-    memset(&n, 0, sizeof(n));
-    mat_copy(n.m, acc);
-    mat_copy(n.t, trans_of(o));
-    n.invert = invert_of(o);
-    switch (t) {
-        case CGS_BOX: {
-            const box* b = (const box*)o;
-            n.op = SJ_CSG_BOX;
-            vec3 c = b->get_center(), f = b->get_offset();
-            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
-            n.p[0] = f.x(), n.p[1] = f.y(), n.p[2] = f.z();
-            break;
-        }
-        case CGS_SPHERE: {
-            const sphere* s = (const sphere*)o;
-            n.op = SJ_CSG_SPHERE;
-            vec3 c = s->get_center();
-            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
-            n.p[0] = s->get_rad();
-            break;
-        }
-        case CGS_CYLINDER: {
-            const cylinder* y = (const cylinder*)o;
-            n.op = SJ_CSG_CYLINDER;
-            vec3 c = y->get_center();
-            n.c[0] = c.x(), n.c[1] = c.y(), n.c[2] = c.z();
-            n.p[0] = y->get_height();
-            n.p[1] = y->*member_of(CylR1());
-            n.p[2] = y->*member_of(CylR2());
-            break;
-        }
-        case CGS_PLANE: {
-            const plane* p = (const plane*)o;
-            n.op = SJ_CSG_PLANE;
-            vec3 v = p->get_normal();
-            n.p[0] = v.x(), n.p[1] = v.y(), n.p[2] = v.z(), n.p[3] = p->get_offset();
-            break;
-        }
-        default: {
-            composite_object* c = (composite_object*)o;
-            const mat3x3 inner = trans_of(o) * acc;  // children see trans_mat * r
-            if (c->get_combine_type() == CGS_CMB_NOOP) {
-                n.op = SJ_CSG_NOOP;
-                break;
-            }
-            const object* l = c->get_child_l();
-            const object* r = c->get_child_r();
-            if (l) flatten(l, c->get_child_type_l(), inner, out);
-            if (r) flatten(r, c->get_child_type_r(), inner, out);
-            // CGS_DIFFERENCE: add_child already set the right child's invert
-            n.op = (l && r) ? (c->get_combine_type() == CGS_UNION ? SJ_CSG_UNION : SJ_CSG_INTERSECT)
-                   : (l || r) ? SJ_CSG_PASS
-                              : SJ_CSG_CONST;
-        }
-    }
-    out.push_back(n);
-}
+// The integration guide's walk, verbatim (mat_copy and flatten).
+#include "guide_flatten.inc"
+
+namespace {
 
 // um_to_l and fs_to_t (src/disp.cpp:5-22): lengths in um and times in fs to
 // the scene's length units, scaled by the context's l_per_um
