@@ -127,3 +127,15 @@ def test_uniform_au_follows_the_ade_recurrence(lib, precision, tol):
     series = f.monitors()[0]
     want = recurrence(1.0, AU, g.dt, 15)
     assert np.max(np.abs(series - want)) <= tol
+
+
+def test_reference_rounding_65_cubed_f64_matches_oracle(lib, oracle_lib):
+    """The junction on the grid the reference's correct_defaults gives the
+    3.2 um cell at 20 px/um (65^3, 20.3125 px/um): an odd nx, so the
+    one-column tile bodies run, over the workload's 2000 steps."""
+    from sim_juncs_gb300.spec import reference_grid
+    g, res = reference_grid(length=2.2, pml_thickness=0.5, resolution=20.0)  # 3.2 um in all
+    assert g.nx == 65 and res == 65 / 3.2
+    inst = junction_instance(n=g.nx, res=res)
+    f = check_against_oracle(inst, 2000, (1, 400))
+    assert gold_field(f, inst) > 0
