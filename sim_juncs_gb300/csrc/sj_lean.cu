@@ -1369,15 +1369,20 @@ constexpr int multi2_minb() { return sizeof(real) == 4 ? SJ_LEAN_MULTI2_MINB : 2
 #ifndef SJ_LEAN_STAGE_MULTI
 #define SJ_LEAN_STAGE_MULTI 1
 #endif
-constexpr bool STAGE_PLAIN = SJ_LEAN_STAGE_PLAIN != 0;
-constexpr bool STAGE_SLAB = SJ_LEAN_STAGE_SLAB != 0;
-constexpr bool STAGE_MULTI = SJ_LEAN_STAGE_MULTI != 0;
+// FP32 only: FP64 steps are bound by the FP64 pipe, not by load latency (and
+// the FP64 plain kernel's stage would not fit the 48 KB default)
 template <typename real>
-constexpr int plain2_smem() { return STAGE_PLAIN ? stage_bytes<real>(0) : 0; }
+constexpr bool stage_plain() { return SJ_LEAN_STAGE_PLAIN != 0 && sizeof(real) == 4; }
 template <typename real>
-constexpr int slab2_smem() { return STAGE_SLAB ? stage_bytes<real>(1) : 0; }
+constexpr bool stage_slab() { return SJ_LEAN_STAGE_SLAB != 0 && sizeof(real) == 4; }
 template <typename real>
-constexpr int multi2_smem() { return STAGE_MULTI ? stage_bytes<real>(3) : 0; }
+constexpr bool stage_multi() { return SJ_LEAN_STAGE_MULTI != 0 && sizeof(real) == 4; }
+template <typename real>
+constexpr int plain2_smem() { return stage_plain<real>() ? stage_bytes<real>(0) : 0; }
+template <typename real>
+constexpr int slab2_smem() { return stage_slab<real>() ? stage_bytes<real>(1) : 0; }
+template <typename real>
+constexpr int multi2_smem() { return stage_multi<real>() ? stage_bytes<real>(3) : 0; }
 
 template <typename real, int ZB>
 __global__ void __launch_bounds__(HALO2_THREADS, slab2_minb<real>())
@@ -1388,11 +1393,11 @@ k_lean_slab2(const __grid_constant__ LeanTable<real> tab) {
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 1)
-        tile_pair_halo_any<real, ZB, 1, STAGE_SLAB>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 1, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
     else if (m == 2)
-        tile_pair_halo_any<real, ZB, 2, STAGE_SLAB>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 2, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
     else
-        tile_pair_halo_any<real, ZB, 4, STAGE_SLAB>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 4, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
 }
 
 template <typename real, int ZB>
@@ -1404,13 +1409,13 @@ k_lean_multi2(const __grid_constant__ LeanTable<real> tab) {
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 3)
-        tile_pair_halo_any<real, ZB, 3, STAGE_MULTI>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 3, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
     else if (m == 5)
-        tile_pair_halo_any<real, ZB, 5, STAGE_MULTI>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 5, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
     else if (m == 6)
-        tile_pair_halo_any<real, ZB, 6, STAGE_MULTI>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 6, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
     else
-        tile_pair_halo_any<real, ZB, 7, STAGE_MULTI>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 7, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
 }
 
 // Plain tiles with two columns per thread (instances whose nx is a multiple
@@ -1422,7 +1427,7 @@ k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
     extern __shared__ __align__(128) unsigned char stg[];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
-    tile_pair_halo_any<real, ZB, 0, STAGE_PLAIN>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol,
+    tile_pair_halo_any<real, ZB, 0, stage_plain<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol,
                                                  stg);
 }
 
