@@ -869,49 +869,9 @@ __device__ __forceinline__ typename Pair<real>::T ld2p(bool on, const real* p, u
     return v;
 }
 
-// Asynchronous global -> shared copies (cp.async, not the TMA unit): N bytes,
-// zero-filled when off (no global read then; src must still be a valid
-// address).  Each thread reads back only what it copied itself, after
-// waiting for its own groups, so no block barrier orders them.
-template <int N>
-__device__ __forceinline__ void cp_async(void* dst, const void* src, bool on) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"(N), "r"(on ? N : 0)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// Staging of the H update's inputs one plane ahead (two stages, by plane
-// parity), structure of arrays so that a warp's accesses are conflict-free:
-// 8 pair fields (E of plane k+1 x, y; Ez; Ez and Ex at y+1; Hx, Hy, Hz), two
-// H-side psi pairs per CPML axis of MASK (x, y, z order), the two E values
-// at column i+2 and the combo word (4 bytes holding the cell pair's bytes).
-template <typename real, int MASK>
-struct StageLay {
-    using V2 = typename Pair<real>::T;
-    static constexpr int T = LX * (LY / 2 + 1);
-    static constexpr int NAX = ((MASK & 1) != 0) + ((MASK & 2) != 0) + ((MASK & 4) != 0);
-    static constexpr int NV = 8 + 2 * NAX;
-    static constexpr int OFF_S = NV * T * (int)sizeof(V2);
-    static constexpr int OFF_C = OFF_S + 2 * T * (int)sizeof(real);
-    static constexpr int BYTES = (OFF_C + T * 4 + 127) / 128 * 128;
-    // first pair field of axis a's H-side psi
-    static constexpr int psi(int a) {
-        return 8 + 2 * ((a > 0 && (MASK & 1)) + (a > 1 && (MASK & 2)));
-    }
-};
-// dynamic shared memory of a pair kernel whose tiles have the masks in `masks`
-template <typename real>
-constexpr int stage_bytes(int max_axes) {
-    return 2 * (((8 + 2 * max_axes) * LX * (LY / 2 + 1) * (int)sizeof(typename Pair<real>::T) +
-                 2 * LX * (LY / 2 + 1) * (int)sizeof(real) + LX * (LY / 2 + 1) * 4 + 127) /
-                128 * 128);
-}
-
-template <typename real, int ZB, int MASK, bool EDGE, bool STG>
+template <typename real, int ZB, int MASK, bool EDGE>
 __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
-                                               HaloPlane<real>* sh, unsigned qf, unsigned char* stg) {
+                                               HaloPlane<real>* sh, unsigned qf) {
     using V2 = typename Pair<real>::T;
     constexpr bool SX = (MASK & 1) != 0, SY = (MASK & 2) != 0, SZ = (MASK & 4) != 0;
     constexpr int NW = LY / 2;  // warps of tile rows
@@ -982,48 +942,6 @@ __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, i
     // a half-warp's 16 lanes take rows 0-15 (three-axis tiles: the z psi rows go without)
     volatile unsigned long long* lr =
         lane_row_park(colh ? 0ull : lane_row<real, SX, SY, SZ>(I, l, xt, yo, qf));
-    // staged: the H update's inputs of plane kk copied asynchronously into
-    // stage kk & 1 (a plane ahead of their use); the same values the direct
-    // loads below read, zero where those are predicated off
-    using L = StageLay<real, MASK>;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    auto stage_issue = [&](int kk, unsigned ok) {
-        constexpr int T = L::T;
-        V2* f = reinterpret_cast<V2*>(stg + (kk & 1) * L::BYTES) + tid;
-        const bool kpk = !EDGE || kk + 1 < nz;
-        const bool zok = SZ && (kk < I.pl[2] || kk >= nz - I.ph[2]);
-        const unsigned opk = ok + qf;
-        constexpr int VB = (int)sizeof(V2);
-        cp_async<VB>(f + 0 * T, eX + (kpk ? ok + plane : ok), kpk);
-        cp_async<VB>(f + 1 * T, eY + (kpk ? ok + plane : ok), kpk);
-        cp_async<VB>(f + 2 * T, eZ + ok, true);
-        cp_async<VB>(f + 3 * T, eZ + (yp ? ok + px : ok), yp);
-        cp_async<VB>(f + 4 * T, eX + (yp ? ok + px : ok), yp);
-        cp_async<VB>(f + 5 * T, hX + ok, true);
-        cp_async<VB>(f + 6 * T, hY + ok, true);
-        cp_async<VB>(f + 7 * T, hZ + ok, true);
-        if (SX) {
-            cp_async<VB>(f + L::psi(0) * T, hiX + opk, xo);
-            cp_async<VB>(f + (L::psi(0) + 1) * T, hiX + opk + vol, xo);
-        }
-        if (SY) {
-            cp_async<VB>(f + L::psi(1) * T, hiY + opk, yo);
-            cp_async<VB>(f + (L::psi(1) + 1) * T, hiY + opk + vol, yo);
-        }
-        if (SZ) {
-            cp_async<VB>(f + L::psi(2) * T, hiZ + opk, zok);
-            cp_async<VB>(f + (L::psi(2) + 1) * T, hiZ + opk + vol, zok);
-        }
-        real* s = reinterpret_cast<real*>(stg + (kk & 1) * L::BYTES + L::OFF_S) + tid;
-        cp_async<(int)sizeof(real)>(s, eZ + (xp2 ? ok + 2 : ok), xp2);
-        cp_async<(int)sizeof(real)>(s + T, eY + (xp2 ? ok + 2 : ok), xp2);
-        unsigned* cw = reinterpret_cast<unsigned*>(stg + (kk & 1) * L::BYTES + L::OFF_C) + tid;
-        cp_async<4>(cw, I.combo + (ok & ~3u), true);
-    };
-    if (STG) {
-        stage_issue(k, o);
-        cp_async_commit();
-    }
     for (; k < z1; ++k, o += plane) {
         const bool kp = !EDGE || k + 1 < nz;
         const bool store = k >= z0;  // block-uniform
@@ -1042,34 +960,14 @@ __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, i
         const unsigned op = o + qf;
         // every load of the H update issued together
         HaloIn2<real> c;
-        real ez_x2l, ey_x2l;
-        unsigned cword = 0;
-        if (STG) {
-            constexpr int T = L::T;
-            cp_async_wait_all();
-            const V2* f = reinterpret_cast<const V2*>(stg + (k & 1) * L::BYTES) + tid;
-            c.ex_n = f[0 * T], c.ey_n = f[1 * T], c.ez = f[2 * T], c.ez_yp = f[3 * T], c.ex_yp = f[4 * T];
-            c.hx = f[5 * T], c.hy = f[6 * T], c.hz = f[7 * T];
-            c.qx0.x = c.qx0.y = c.qx1.x = c.qx1.y = real(0);
-            c.qy0 = c.qx0, c.qy1 = c.qx0, c.qz0 = c.qx0, c.qz1 = c.qx0;
-            if (SX) c.qx0 = f[L::psi(0) * T], c.qx1 = f[(L::psi(0) + 1) * T];
-            if (SY) c.qy0 = f[L::psi(1) * T], c.qy1 = f[(L::psi(1) + 1) * T];
-            if (SZ) c.qz0 = f[L::psi(2) * T], c.qz1 = f[(L::psi(2) + 1) * T];
-            const real* s = reinterpret_cast<const real*>(stg + (k & 1) * L::BYTES + L::OFF_S) + tid;
-            ez_x2l = s[0], ey_x2l = s[T];
-            cword = reinterpret_cast<const unsigned*>(stg + (k & 1) * L::BYTES + L::OFF_C)[tid];
-            if (k + 1 < z1) stage_issue(k + 1, o + plane);
-            cp_async_commit();
-        } else {
-            c.ex_n = ld2p(kp, eX, o + plane), c.ey_n = ld2p(kp, eY, o + plane);
-            c.ez = ld2(eZ, o);
-            c.ez_yp = ld2p(yp, eZ, o + px), c.ex_yp = ld2p(yp, eX, o + px);
-            c.hx = ld2(hX, o), c.hy = ld2(hY, o), c.hz = ld2(hZ, o);
-            c.qy0 = ld2p(SY && yo, hiY, op), c.qy1 = ld2p(SY && yo, hiY, op + vol);
-            c.qz0 = ld2p(SZ && zo, hiZ, op), c.qz1 = ld2p(SZ && zo, hiZ, op + vol);
-            c.qx0 = ld2p(SX && xo, hiX, op), c.qx1 = ld2p(SX && xo, hiX, op + vol);
-            ez_x2l = xp2 ? ldg(eZ, o + 2) : real(0), ey_x2l = xp2 ? ldg(eY, o + 2) : real(0);
-        }
+        c.ex_n = ld2p(kp, eX, o + plane), c.ey_n = ld2p(kp, eY, o + plane);
+        c.ez = ld2(eZ, o);
+        c.ez_yp = ld2p(yp, eZ, o + px), c.ex_yp = ld2p(yp, eX, o + px);
+        c.hx = ld2(hX, o), c.hy = ld2(hY, o), c.hz = ld2(hZ, o);
+        c.qy0 = ld2p(SY && yo, hiY, op), c.qy1 = ld2p(SY && yo, hiY, op + vol);
+        c.qz0 = ld2p(SZ && zo, hiZ, op), c.qz1 = ld2p(SZ && zo, hiZ, op + vol);
+        c.qx0 = ld2p(SX && xo, hiX, op), c.qx1 = ld2p(SX && xo, hiX, op + vol);
+        const real ez_x2l = xp2 ? ldg(eZ, o + 2) : real(0), ey_x2l = xp2 ? ldg(eY, o + 2) : real(0);
         {
             const real a = __shfl_down_sync(FULL, c.ez.x, 1, 16), b = __shfl_down_sync(FULL, ey_c.x, 1, 16);
             c.ez_x2 = xl ? ez_x2l : a;
@@ -1114,13 +1012,7 @@ __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, i
             // combos and the old E-side psi (the combo loads are unconditional:
             // every thread's offset is a cell pair of the grid)
             const bool eo = own && act;
-            uchar2 cb;
-            if (STG) {
-                const unsigned h = (o & 2u) ? (cword >> 16) : (cword & 0xffffu);
-                cb.x = (unsigned char)(h & 255u), cb.y = (unsigned char)(h >> 8);
-            } else {
-                cb = __ldg(reinterpret_cast<const uchar2*>(I.combo + o));
-            }
+            const uchar2 cb = __ldg(reinterpret_cast<const uchar2*>(I.combo + o));
             const real* s0 = I.coef + (int)cb.x * I.ncoef + I.ncoef - 3;
             const real* s1 = I.coef + (int)cb.y * I.ncoef + I.ncoef - 3;
             const real a0 = ldg(s0, 0), a1 = ldg(s0, 1), a2 = ldg(s0, 2);
@@ -1195,13 +1087,13 @@ __device__ __forceinline__ void tile_pair_halo(const InstDev<real>& I, int tx, i
     }
 }
 
-template <typename real, int ZB, int MASK, bool STG>
+template <typename real, int ZB, int MASK>
 __device__ __forceinline__ void tile_pair_halo_any(const InstDev<real>& I, int tx, int ty, int tz, bool dry,
-                                                   HaloPlane<real>* sh, unsigned qf, unsigned char* stg) {
+                                                   HaloPlane<real>* sh, unsigned qf) {
     if (tile_edge(I, tx, ty, tz, ZB))
-        tile_pair_halo<real, ZB, MASK, true, STG>(I, tx, ty, tz, dry, sh, qf, stg);
+        tile_pair_halo<real, ZB, MASK, true>(I, tx, ty, tz, dry, sh, qf);
     else
-        tile_pair_halo<real, ZB, MASK, false, STG>(I, tx, ty, tz, dry, sh, qf, stg);
+        tile_pair_halo<real, ZB, MASK, false>(I, tx, ty, tz, dry, sh, qf);
 }
 
 
@@ -1357,65 +1249,36 @@ constexpr int slab2_minb() { return sizeof(real) == 4 ? SJ_LEAN_SLAB2_MINB : 2; 
 template <typename real>
 constexpr int multi2_minb() { return sizeof(real) == 4 ? SJ_LEAN_MULTI2_MINB : 2; }
 
-// Two-column kernels that stage the H update's inputs a plane ahead with
-// cp.async (dynamic shared memory stage_bytes) instead of loading them when
-// the plane starts; 1 = staged.
-#ifndef SJ_LEAN_STAGE_PLAIN
-#define SJ_LEAN_STAGE_PLAIN 1
-#endif
-#ifndef SJ_LEAN_STAGE_SLAB
-#define SJ_LEAN_STAGE_SLAB 1
-#endif
-#ifndef SJ_LEAN_STAGE_MULTI
-#define SJ_LEAN_STAGE_MULTI 1
-#endif
-// FP32 only: FP64 steps are bound by the FP64 pipe, not by load latency (and
-// the FP64 plain kernel's stage would not fit the 48 KB default)
-template <typename real>
-constexpr bool stage_plain() { return SJ_LEAN_STAGE_PLAIN != 0 && sizeof(real) == 4; }
-template <typename real>
-constexpr bool stage_slab() { return SJ_LEAN_STAGE_SLAB != 0 && sizeof(real) == 4; }
-template <typename real>
-constexpr bool stage_multi() { return SJ_LEAN_STAGE_MULTI != 0 && sizeof(real) == 4; }
-template <typename real>
-constexpr int plain2_smem() { return stage_plain<real>() ? stage_bytes<real>(0) : 0; }
-template <typename real>
-constexpr int slab2_smem() { return stage_slab<real>() ? stage_bytes<real>(1) : 0; }
-template <typename real>
-constexpr int multi2_smem() { return stage_multi<real>() ? stage_bytes<real>(3) : 0; }
-
 template <typename real, int ZB>
 __global__ void __launch_bounds__(HALO2_THREADS, slab2_minb<real>())
 k_lean_slab2(const __grid_constant__ LeanTable<real> tab) {
     __shared__ HaloPlane<real> sh[2];
-    extern __shared__ __align__(128) unsigned char stg[];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 1)
-        tile_pair_halo_any<real, ZB, 1, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 1>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 2)
-        tile_pair_halo_any<real, ZB, 2, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 2>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else
-        tile_pair_halo_any<real, ZB, 4, stage_slab<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 4>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
 }
 
 template <typename real, int ZB>
 __global__ void __launch_bounds__(HALO2_THREADS, multi2_minb<real>())
 k_lean_multi2(const __grid_constant__ LeanTable<real> tab) {
     __shared__ HaloPlane<real> sh[2];
-    extern __shared__ __align__(128) unsigned char stg[];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
     const unsigned qf = blockIdx.y * tab.qvol;
     if (m == 3)
-        tile_pair_halo_any<real, ZB, 3, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 3>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 5)
-        tile_pair_halo_any<real, ZB, 5, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 5>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else if (m == 6)
-        tile_pair_halo_any<real, ZB, 6, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 6>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
     else
-        tile_pair_halo_any<real, ZB, 7, stage_multi<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf, stg);
+        tile_pair_halo_any<real, ZB, 7>(tab.inst, tx, ty, tz, tab.dry != 0, sh, qf);
 }
 
 // Plain tiles with two columns per thread (instances whose nx is a multiple
@@ -1424,11 +1287,9 @@ template <typename real, int ZB>
 __global__ void __launch_bounds__(HALO2_THREADS, pair_plain_minb<real>())
 k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
     __shared__ HaloPlane<real> sh[2];
-    extern __shared__ __align__(128) unsigned char stg[];
     int tx, ty, tz, m;
     tile_decode(__ldg(tab.tiles + blockIdx.x), tx, ty, tz, m);
-    tile_pair_halo_any<real, ZB, 0, stage_plain<real>()>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol,
-                                                 stg);
+    tile_pair_halo_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol);
 }
 
 // General tiles (an H source in the footprint) and probe blocks of every
@@ -1667,21 +1528,18 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
         t.tiles = T.list[LEAN_MULTI], t.n_tiles = T.count[LEAN_MULTI];                                       \
         if constexpr (sizeof(real) == 4)                                                                     \
             if (t.n_tiles && pairs2)                                                                         \
-                k_lean_multi2<real, Z>                                                                       \
-                    <<<dim3((unsigned)t.n_tiles, gn), halo2, multi2_smem<real>(), sc[LEAN_MULTI]>>>(t);      \
+                k_lean_multi2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_MULTI]>>>(t);      \
         if (t.n_tiles && !pairs2)                                                                            \
             k_lean_multi<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_MULTI]>>>(t);            \
         t.tiles = T.list[LEAN_SLAB], t.n_tiles = T.count[LEAN_SLAB];                                         \
         if constexpr (sizeof(real) == 4)                                                                     \
             if (t.n_tiles && pairs2)                                                                         \
-                k_lean_slab2<real, Z>                                                                        \
-                    <<<dim3((unsigned)t.n_tiles, gn), halo2, slab2_smem<real>(), sc[LEAN_SLAB]>>>(t);        \
+                k_lean_slab2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_SLAB]>>>(t);        \
         if (t.n_tiles && !pairs2)                                                                            \
             k_lean_slab<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo, 0, sc[LEAN_SLAB]>>>(t);              \
         t.tiles = T.list[LEAN_PLAIN], t.n_tiles = T.count[LEAN_PLAIN];                                       \
         if (t.n_tiles && pairs)                                                                              \
-            k_lean_plain2<real, Z>                                                                           \
-                <<<dim3((unsigned)t.n_tiles, gn), halo2, plain2_smem<real>(), sc[LEAN_PLAIN]>>>(t);          \
+            k_lean_plain2<real, Z><<<dim3((unsigned)t.n_tiles, gn), halo2, 0, sc[LEAN_PLAIN]>>>(t);          \
         if (t.n_tiles && !pairs)                                                                             \
             k_lean_plain<real, Z><<<dim3((unsigned)t.n_tiles, gn), block, 0, sc[LEAN_PLAIN]>>>(t);           \
         break;
