@@ -8,6 +8,11 @@ junction192 (one 192^3 sweep member), junction192x4 (four 192^3 sweep
 members: one launch group, ~3.4 GB on the device), bowtie (512 x 512 x
 384), junction64 (64^3).  Prints the launches per step so that a capture
 can skip set-up launches and warm-up steps by count.
+
+--diag energy: after the steps, three sj_energy calls (k_energy + k_sum);
+--diag phases: then the phases of 384 monitor series (the sweep's 96 x 4
+gap points, here 48 copies of the 64^3 junction's 8) in one sj_extract_phases
+call (k_phases).
 """
 import argparse
 
@@ -36,6 +41,7 @@ def main():
     p.add_argument("--schedule", default=None)
     p.add_argument("--zseg", type=int, default=8)
     p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--diag", default=None, choices=["energy", "phases"])
     a = p.parse_args()
     f = Fields(instances(a.workload), a.precision, a.schedule)
     if f.schedule_name() == "fused":
@@ -44,6 +50,16 @@ def main():
     f.synchronize()
     print(f"{a.workload} {a.precision} {f.schedule_name()} steps={f.steps_done} voxels={f.voxels()} "
           f"launches_per_step={f.launches_per_step()}", flush=True)
+    if a.diag == "energy":
+        for _ in range(3):
+            print("energy", f.energy(0), flush=True)
+    elif a.diag == "phases":
+        import numpy as np
+        from .phases import extract_phases
+        mon = f.monitors(0)
+        t = np.arange(mon.shape[1]) * (f.instances[0].grid.dt * f.instances[0].save_span)
+        res = extract_phases(t, np.tile(mon, (48, 1)), 2.0)
+        print("phases", len(res), sum(r["status"] == 0 for r in res), flush=True)
     f.close()
 
 
