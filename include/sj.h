@@ -527,7 +527,9 @@ enum {
                                    f0, phi, t0_corr and the band are valid */
     SJ_PHASE_EMPTY_BAND = 2,    /* zero-width band (the recentring test divides by it) */
     SJ_PHASE_BAD_F0 = 3,        /* no finite central frequency inside the spectrum */
-    SJ_PHASE_BAD_T0 = 4         /* recentring moved t0 outside the series */
+    SJ_PHASE_BAD_T0 = 4,        /* recentring moved t0 outside the series */
+    SJ_PHASE_WIDE_BAND = 5      /* a band of more than 256 bins (the kernel's fit size; the
+                                   reference has no such limit) */
 };
 typedef struct {
     double f0;                  /* central frequency (signal.f0) */

@@ -103,7 +103,7 @@ class PhaseResult(C.Structure):
                 ("lowpass_steps", C.c_int32), ("status", C.c_int32), ("_pad", C.c_int32)]
 
 
-PHASE_OK, PHASE_NARROW_BAND, PHASE_EMPTY_BAND, PHASE_BAD_F0, PHASE_BAD_T0 = range(5)
+PHASE_OK, PHASE_NARROW_BAND, PHASE_EMPTY_BAND, PHASE_BAD_F0, PHASE_BAD_T0, PHASE_WIDE_BAND = range(6)
 
 STRUCTS = {0: GridDesc, 1: Pole, 2: CsgNode, 3: RegionDesc, 4: SceneDesc, 5: MaterialDesc,
            6: PmlDesc, 7: SourceDesc, 8: ProbeDesc, 9: InstanceDesc, 10: DesignDesc, 11: ObjectiveDesc,

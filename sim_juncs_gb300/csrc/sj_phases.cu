@@ -444,7 +444,7 @@ k_phases(const double* __restrict__ vin, long long s_series, long long s_sample,
             } else {
                 double slope, icpt;
                 if (n > 256) {
-                    C.status = SJ_PHASE_BAD_F0;
+                    C.status = SJ_PHASE_WIDE_BAND;
                 } else {
                     band_regression(vf, C.f_min, C.f_max, df, scratch, &slope, &icpt);
                     C.t0_corr = -slope / (2 * PI);
@@ -505,7 +505,7 @@ k_phases(const double* __restrict__ vin, long long s_series, long long s_sample,
         freq_band(mags, M, C.f0_ind, CUT_ALPHA, &C.f_min, &C.f_max);
         const int n = C.f_max - C.f_min;
         if (n < 5 || n > 256) {
-            C.status = n < 5 ? SJ_PHASE_NARROW_BAND : SJ_PHASE_BAD_F0;
+            C.status = n < 5 ? SJ_PHASE_NARROW_BAND : SJ_PHASE_WIDE_BAND;
         } else {
             for (int i = 0; i < n; ++i) scratch[i] = atan2(vf[C.f_min + i].y, vf[C.f_min + i].x);
             fix_angle_seq(scratch, n);
