@@ -433,8 +433,10 @@ k_phases(const double* __restrict__ vin, long long s_series, long long s_sample,
         apply_lowpass(vf0, N, M, df, C.last_cent, C.low_stren, C.t0_ind, vf, mags, v);
     }
     // _param_est, recentred at most once
-    for (int pass = 0; pass < 2 && !C.status; ++pass) {
-        if (threadIdx.x == 0) {
+    // (the loop reads the control words only after a barrier: thread 0 writes
+    // them at the top of a pass while the others wait)
+    for (int pass = 0; pass < 2; ++pass) {
+        if (threadIdx.x == 0 && !C.status) {
             C.go = 0;
             freq_band(mags, M, C.f0_ind, CUT_ALPHA, &C.f_min, &C.f_max);
             const int n = C.f_max - C.f_min;
