@@ -443,7 +443,13 @@ int sj_divergence(const sj_sim* sim, int64_t* step, int32_t* inst, int32_t* moni
    to regenerate what the gradient needs.  d_obj_d_eps receives, instance
    after instance, dF/d(eps) for every design voxel ([n2][n1][n0] order);
    obj receives F per instance.  On return the instances hold the state
-   after N steps. */
+   after N steps.  Memory: (N / checkpoint_every + 1) copies of the full
+   state (fields, CPML psi, polarisations) plus the E-update bracket at the
+   design points for checkpoint_every steps; the work does not depend on
+   the interval (each segment is re-run once).  checkpoint_every <= 0 or
+   >= N keeps one segment: two state copies and the bracket of all N steps,
+   the least memory whenever the design region is small.  An interval whose
+   copies do not fit the free device memory fails with SJ_E_NOMEM. */
 typedef struct {
     int32_t lo[3];              /* first voxel of the design box */
     int32_t n[3];               /* extent in voxels */

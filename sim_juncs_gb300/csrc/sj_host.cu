@@ -1492,6 +1492,17 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
     size_t sbytes = 0;
     for (const Arr& a : state_of(0)) sbytes += a.bytes;
     const long long nseg = (N + K - 1) / K;
+    {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && (size_t)(nseg + 1) * sbytes > free_b) {
+            char buf[240];
+            snprintf(buf, sizeof buf,
+                     "the %lld checkpoints of %.2f GB each need %.1f GB, %.1f GB are free: use a larger "
+                     "checkpoint_every (<= 0: one segment)",
+                     nseg + 1, sbytes / 1e9, (nseg + 1) * (double)sbytes / 1e9, free_b / 1e9);
+            fail(SJ_E_NOMEM, buf);
+        }
+    }
     char* arena = (char*)tmp((size_t)(nseg + 1) * sbytes);
     std::vector<int> slot_cur(nseg + 1, 0);  // the parity each checkpoint was taken at
     auto save = [&](long long slot) {
