@@ -45,7 +45,8 @@ extern "C" {
 
 /* raised whenever a struct layout or a signature changes; 2: sj_scene_desc
    gained smooth_n and smooth_rad; 3: the divergence guard, bounded-wait,
-   energy, flux and phase-extraction entry points and sj_phase_result */
+   energy, flux, phase-extraction and fused launch-mode entry points and
+   sj_phase_result */
 #define SJ_ABI_VERSION 3
 
 /* status codes */
@@ -293,6 +294,19 @@ int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* ring, int32_t* zs
    everywhere.  Both evaluate the same per-cell arithmetic in the same order:
    the results do not change. */
 int sj_set_fused_columns(sj_sim* sim, int32_t columns);
+/* FUSED: how a step's tile kernels are launched.  GROUPED (default): one
+   launch per launch group and tile class (plain, single-slab, multi-slab),
+   the launches of a step concurrent on forked streams.  QUEUE: one launch of
+   resident blocks for every group's tiles, which claim (group, member, tile)
+   items from a counter, multi-slab tiles first; FP32 with two columns per
+   thread only (every instance's nx a multiple of 32), else the grouped
+   launches run.  Both evaluate the same per-cell arithmetic: the results do
+   not change.  sj_autotune tries both where QUEUE applies and keeps the
+   faster. */
+enum { SJ_LAUNCH_GROUPED = 0, SJ_LAUNCH_QUEUE = 1 };
+int sj_set_fused_launch(sj_sim* sim, int32_t mode);
+/* the launch mode in use (SJ_LAUNCH_*), -1 for a null handle */
+int32_t sj_get_fused_launch(const sj_sim* sim);
 /* time every fused tiling with `steps` launches that leave the state
    untouched, keep the fastest and report it (any output may be NULL) */
 int sj_autotune(sj_sim* sim, int32_t steps, int32_t* tile_y, int32_t* ring, int32_t* zseg,

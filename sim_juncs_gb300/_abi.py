@@ -21,6 +21,7 @@ EX, EY, EZ, HX, HY, HZ = range(6)
 COMPONENTS = {"Ex": EX, "Ey": EY, "Ez": EZ, "Hx": HX, "Hy": HY, "Hz": HZ}
 F64, F32 = 0, 1
 SCHED_FUSED, SCHED_SPLIT, SCHED_TMA = 0, 1, 2
+LAUNCH_GROUPED, LAUNCH_QUEUE = 0, 1
 SRC_GAUSSIAN, SRC_CONTINUOUS = 0, 1
 PROBE_MONITOR, PROBE_DFT = 1, 2
 CSG_BOX, CSG_SPHERE, CSG_CYLINDER, CSG_PLANE = 0, 1, 2, 3
@@ -151,6 +152,8 @@ SIGNATURES = {
     "sj_read_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),
     "sj_set_snapshots": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "sj_set_fused_columns": (C.c_int, [_P, C.c_int32]),
+    "sj_set_fused_launch": (C.c_int, [_P, C.c_int32]),
+    "sj_get_fused_launch": (C.c_int32, [_P]),
     "sj_take_snapshot": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64), _D, C.c_size_t]),
     "sj_snapshots_pending": (C.c_int32, [_P, C.c_int32]),
     "sj_write_field": (C.c_int, [_P, C.c_int32, C.c_int32, _D, C.c_size_t]),

@@ -179,6 +179,15 @@ struct sj_sim {
     void* d_parity = nullptr;          // every instance descriptor twice, by parity (LeanGen)
     cudaStream_t side[LEAN_STREAMS] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[LEAN_STREAMS] = {};
+    std::vector<unsigned> h_tiles;     // host copy of the tile lists (prepare_lean)
+    std::vector<long long> h_tile_off; // [instance][class] offset into h_tiles
+    // queued launch of the fused schedule (SJ_LAUNCH_QUEUE)
+    int l_launch = SJ_LAUNCH_GROUPED;
+    LeanQueue<float> queue{};
+    std::vector<LeanTable<float>> q_tabs;  // [dry][parity][group] descriptors (host; kernel parameters)
+    void* d_qitems = nullptr;
+    long long q_version = -1;          // table_version the queue tables were built from
+    int q_zb = -1;                     // z-segment length the queue items were built for
     // dump_raw snapshots (per instance) and the stream their host copies run on
     std::vector<Snapshots> snaps;
     cudaStream_t copy_stream = nullptr;
@@ -1015,6 +1024,8 @@ void prepare_lean(sj_sim* sim) {
                 first = r;
             }
     }
+    sim->h_tiles = all;
+    sim->h_tile_off = off;
     sim->dfree(sim->d_tiles);
     sim->d_tiles = sim->upload(all);
     const unsigned* base = reinterpret_cast<const unsigned*>(sim->d_tiles);
@@ -1045,10 +1056,88 @@ void prepare_lean(sj_sim* sim) {
     sim->lean_zb = sim->l_zb;
 }
 
+// Can the fused schedule's tiles run as one queued launch?  FP32, two
+// columns per thread, every instance with whole 32-column rows.
+template <typename real>
+bool queue_eligible(sj_sim* sim) {
+    if (sizeof(real) != 4 || sim->l_one_column) return false;
+    for (const auto& I : devv<real>(sim))
+        if (I.nx % 32 != 0) return false;
+    return true;
+}
+
+// The queued launch's descriptor tables and items for the current tile lists
+// and descriptors (rebuilt when either changes); nullptr when the grouped
+// launches run.
+template <typename real>
+const LeanQueue<real>* prepare_queue(sj_sim* sim) {
+    if constexpr (sizeof(real) != 4) {
+        return nullptr;
+    } else {
+        if (sim->l_launch != SJ_LAUNCH_QUEUE || !queue_eligible<real>(sim)) return nullptr;
+        if (sim->q_version == sim->table_version && sim->q_zb == sim->lean_zb) return &sim->queue;
+        const auto& dv = devv<float>(sim);
+        const int ng = (int)sim->lgroups.size();
+        // [dry][parity][group]
+        if (ng > LEAN_QUEUE_GROUPS) return nullptr;  // more groups than one launch's parameters hold
+        std::vector<LeanTable<float>>& tabs = sim->q_tabs;
+        tabs.assign(4 * (size_t)ng, LeanTable<float>{});
+        for (int dry = 0; dry < 2; ++dry)
+            for (int par = 0; par < 2; ++par)
+                for (int g = 0; g < ng; ++g) {
+                    LeanTable<float>& t = tabs[((size_t)dry * 2 + par) * ng + g];
+                    memset(&t, 0, sizeof(t));
+                    t.inst = dv[sim->lgroups[g].lead];
+                    if (par) {
+                        for (int c = 0; c < 6; ++c) std::swap(t.inst.F[0][c], t.inst.F[1][c]);
+                        for (int a = 0; a < 3; ++a) std::swap(t.inst.psiH[0][a], t.inst.psiH[1][a]);
+                    }
+                    t.dry = dry;
+                    t.qvol = (unsigned)t.inst.vol;
+                }
+        // items: multi-slab tiles of every group, then single-slab, then plain;
+        // groups of larger grids first, members in order
+        std::vector<int> order(ng);
+        for (int g = 0; g < ng; ++g) order[g] = g;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return dv[sim->lgroups[a].lead].vol > dv[sim->lgroups[b].lead].vol; });
+        std::vector<uint4> items;
+        for (int cls : {LEAN_MULTI, LEAN_SLAB, LEAN_PLAIN})
+            for (int g : order) {
+                const int lead = sim->lgroups[g].lead;
+                const long long o = sim->h_tile_off[(size_t)lead * LEAN_CLASSES + cls];
+                const long long n = sim->ltiles[lead].count[cls];
+                for (int r = 0; r < sim->lgroups[g].n; ++r)
+                    for (long long t = 0; t < n; ++t)
+                        items.push_back(make_uint4((unsigned)g, (unsigned)r, sim->h_tiles[(size_t)(o + t)], 0u));
+            }
+        if (items.size() >= (1ull << 32)) fail(SJ_E_INVALID, "too many tiles for the queued launch");
+        sim->dfree(sim->d_qitems);
+        sim->d_qitems = items.empty() ? nullptr : sim->upload(items);
+        if (!sim->queue.ctr) sim->queue.ctr = (unsigned*)sim->dalloc(sizeof(unsigned));
+        int dev = 0, sms = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        const int nb = lean_queue_blocks_per_sm(sim->lean_zb);
+        if (nb < 1) fail(SJ_E_CUDA, "queued tile kernel cannot be resident");
+        sim->queue.tabs = tabs.data();
+        sim->queue.items = reinterpret_cast<const uint4*>(sim->d_qitems);
+        sim->queue.n_items = (unsigned)items.size();
+        sim->queue.n_groups = ng;
+        sim->queue.grid = nb * sms;
+        sim->q_version = sim->table_version;
+        sim->q_zb = sim->lean_zb;
+        return &sim->queue;
+    }
+}
+
 template <typename real>
 void prepare_schedule(sj_sim* sim) {
     if (sim->schedule == SJ_SCHED_TMA) prepare_fused<real>(sim);
-    if (sim->schedule == SJ_SCHED_FUSED) prepare_lean<real>(sim);
+    if (sim->schedule == SJ_SCHED_FUSED) {
+        prepare_lean<real>(sim);
+        prepare_queue<real>(sim);
+    }
 }
 
 // Side streams and events of the fused schedule, created on first use.
@@ -1081,9 +1170,10 @@ cudaError_t launch_one(sj_sim* sim) {
     cudaError_t e;
     if (sim->schedule == SJ_SCHED_FUSED) {
         prepare_lean<real>(sim);
+        const LeanQueue<real>* q = prepare_queue<real>(sim);
         e = launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), sim->ltiles.data(), sim->lgroups.data(),
                                    (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, sim->l_zb, 0, sim->cur,
-                                   sim->d_state, lean_streams(sim), sim->l_one_column);
+                                   sim->d_state, lean_streams(sim), sim->l_one_column, q);
     } else if (sim->schedule == SJ_SCHED_TMA) {
         prepare_fused<real>(sim);
         e = launch_fused_step<real>(d, sim->n_inst, sim->d_state, sim->fl, sim->stream);
@@ -1102,26 +1192,32 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
     const int zbs[3] = {8, 16, 32};
     float best = 1e30f;
     int bzb = sim->l_zb;
+    // the queued launch is a candidate where it applies
+    const bool try_queue = queue_eligible<real>(sim);
+    int blaunch = sim->l_launch;
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     ensure_capacity<real>(sim, sim->t + 1);
     const auto& dv = devv<real>(sim);
     const LeanStreams ls = lean_streams(sim);
+    for (int mode = 0; mode < (try_queue ? 2 : 1); ++mode)
     for (int zb : zbs) {
         sim->l_zb = zb;
+        if (try_queue) sim->l_launch = mode;
         prepare_lean<real>(sim);
+        const LeanQueue<real>* qu = prepare_queue<real>(sim);
         const LeanTiles* lt = sim->ltiles.data();
         const InstDev<real>* d = reinterpret_cast<const InstDev<real>*>(sim->d_table);
         ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
                                   (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
-                                  sim->d_state, ls, sim->l_one_column),
+                                  sim->d_state, ls, sim->l_one_column, qu),
            "autotune");
         ck(cudaEventRecord(e0, sim->stream), "event");
         for (int q = 0; q < steps; ++q)
             ck(launch_lean_step<real>(dv.data(), d, parity_table<real>(sim), lt, sim->lgroups.data(),
                                       (int)sim->lgroups.size(), sim->lgen, sim->lfix, sim->n_inst, zb, 1, sim->cur,
-                                      sim->d_state, ls, sim->l_one_column),
+                                      sim->d_state, ls, sim->l_one_column, qu),
                "autotune");
         ck(cudaEventRecord(e1, sim->stream), "event");
         ck(cudaEventSynchronize(e1), "event");
@@ -1130,12 +1226,16 @@ void autotune_lean(sj_sim* sim, int steps, int* best_zs, float* best_ms) {
         if (ms < best) {
             best = ms;
             bzb = zb;
+            blaunch = sim->l_launch;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     sim->l_zb = bzb;
+    sim->l_launch = blaunch;
+    sim->drop_graphs();
     prepare_lean<real>(sim);
+    prepare_queue<real>(sim);
     if (best_zs) *best_zs = bzb;
     if (best_ms) *best_ms = best / steps;
 }
@@ -1905,6 +2005,24 @@ int sj_set_fused_columns(sj_sim* sim, int32_t columns) {
     return SJ_OK;
 }
 
+int sj_set_fused_launch(sj_sim* sim, int32_t mode) {
+    if (!sim) return SJ_E_INVALID;
+    if (mode != SJ_LAUNCH_GROUPED && mode != SJ_LAUNCH_QUEUE) return finish(sim, SJ_E_INVALID, "bad launch mode");
+    SJ_TRY(sim)
+    if (mode == SJ_LAUNCH_QUEUE) {
+        const bool ok = sim->precision == SJ_F32 ? queue_eligible<float>(sim) : false;
+        if (!ok)
+            fail(SJ_E_INVALID, "the queued launch runs FP32 two-column tiles: every instance's nx must be a "
+                               "multiple of 32 and one column per thread off");
+    }
+    ck(cudaStreamSynchronize(sim->stream), "sync");
+    sim->l_launch = mode;
+    sim->drop_graphs();
+    SJ_CATCH(sim)
+}
+
+int32_t sj_get_fused_launch(const sj_sim* sim) { return sim ? sim->l_launch : -1; }
+
 int sj_get_tiling(const sj_sim* sim, int32_t* tile_y, int32_t* ring, int32_t* zseg) {
     if (!sim || !tile_y || !ring || !zseg) return SJ_E_INVALID;
     if (sim->schedule == SJ_SCHED_FUSED) {
@@ -2050,6 +2168,16 @@ int32_t sj_launches_per_step(const sj_sim* sim) {
         for (int p = 0; p < LEAN_FIX_PASSES; ++p) fx.count[p] = (long long)passes[p].size();
         const LeanGroup* lg = sim->lgroups.data();
         const int ng = (int)sim->lgroups.size();
+        sj_sim* ms = const_cast<sj_sim*>(sim);
+        if (sim->precision == SJ_F32 && sim->l_launch == SJ_LAUNCH_QUEUE && queue_eligible<float>(ms) &&
+            ng <= LEAN_QUEUE_GROUPS) {
+            // one queued launch for every group's plain, slab and multi tiles
+            int total = 1;
+            for (int p = 0; p < LEAN_FIX_PASSES; ++p) total += fx.count[p] > 0;
+            for (int q = 0; q < sim->n_inst; ++q)
+                if (lt[q].count[LEAN_PLAIN] + lt[q].count[LEAN_SLAB] + lt[q].count[LEAN_MULTI] > 0) return total + 1;
+            return total;
+        }
         return lean_launches(lt.data(), lg, ng, fx);
     }
     if (sim->schedule == SJ_SCHED_TMA) return 1;

@@ -204,11 +204,31 @@ struct LeanStreams {
     cudaStream_t side[LEAN_STREAMS];
     cudaEvent_t fork, join[LEAN_STREAMS];
 };
+// Queued launch of the fused schedule (FP32, every instance with whole
+// 32-column rows): the plain, slab and multi-slab tiles of every group in one
+// launch of resident blocks that claim tiles from a counter, multi-slab tiles
+// first, then single-slab, then plain.
+constexpr int LEAN_QUEUE_GROUPS = 16;  // most launch groups one queued launch takes
+template <typename real>
+struct LeanQueueParams {          // kernel parameter: every group's descriptor
+    LeanTable<real> t[LEAN_QUEUE_GROUPS];
+};
+template <typename real>
+struct LeanQueue {
+    const LeanTable<real>* tabs;   // host [dry][parity][group]: the descriptors with the parity applied
+    const uint4* items;            // (group, member, tile code, 0) in claiming order
+    unsigned n_items;
+    unsigned* ctr;                 // items claimed; zeroed before each launch
+    int n_groups;
+    int grid;                      // resident blocks per SM x SMs
+};
+int lean_queue_blocks_per_sm(int zb);   // occupancy of the queued kernel (FP32)
 template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
                              const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
                              int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls, int one_column = 0);
+                             int cur, DevState* st, const LeanStreams& ls, int one_column = 0,
+                             const LeanQueue<real>* queue = nullptr);
 template <typename real>
 int fused_box_width();          // TMA box width in elements (x)
 template <typename real>

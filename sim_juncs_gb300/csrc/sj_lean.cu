@@ -1292,6 +1292,58 @@ k_lean_plain2(const __grid_constant__ LeanTable<real> tab) {
     tile_pair_halo_any<real, ZB, 0>(tab.inst, tx, ty, tz, tab.dry != 0, sh, blockIdx.y * tab.qvol);
 }
 
+// Queued tiles (LeanQueue): resident blocks claim (group, member, tile)
+// items from a counter, multi-slab tiles first; every group's descriptor
+// travels in the parameter space (as the grouped launches' one does), and the
+// tile runs the two-column body of its slab mask.  One register budget covers
+// every mask.
+#ifndef SJ_LEAN_QUEUE_MINB
+#define SJ_LEAN_QUEUE_MINB 5
+#endif
+template <typename real, int ZB>
+__global__ void __launch_bounds__(HALO2_THREADS, SJ_LEAN_QUEUE_MINB)
+k_lean_queue(const __grid_constant__ LeanQueueParams<real> qp, const uint4* __restrict__ items, unsigned n_items,
+             unsigned* __restrict__ ctr) {
+    __shared__ HaloPlane<real> sh[2];
+    __shared__ unsigned s_item;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (;;) {
+        __syncthreads();  // the previous tile is done with sh
+        if (tid == 0) s_item = atomicAdd(ctr, 1u);
+        __syncthreads();
+        const unsigned it = s_item;
+        if (it >= n_items) break;
+        const uint4 w = __ldg(items + it);
+        const LeanTable<real>& st = qp.t[w.x];
+        int tx, ty, tz, m;
+        tile_decode(w.z, tx, ty, tz, m);
+        const unsigned qf = w.y * st.qvol;
+        const bool dry = st.dry != 0;
+        switch (m) {
+            case 0: tile_pair_halo_any<real, ZB, 0>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 1: tile_pair_halo_any<real, ZB, 1>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 2: tile_pair_halo_any<real, ZB, 2>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 3: tile_pair_halo_any<real, ZB, 3>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 4: tile_pair_halo_any<real, ZB, 4>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 5: tile_pair_halo_any<real, ZB, 5>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            case 6: tile_pair_halo_any<real, ZB, 6>(st.inst, tx, ty, tz, dry, sh, qf); break;
+            default: tile_pair_halo_any<real, ZB, 7>(st.inst, tx, ty, tz, dry, sh, qf); break;
+        }
+    }
+}
+
+int lean_queue_blocks_per_sm(int zb) {
+    int nb = 0;
+    cudaError_t e = cudaSuccess;
+    if (zb == 8)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lean_queue<float, 8>, HALO2_THREADS, 0);
+    else if (zb == 16)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lean_queue<float, 16>, HALO2_THREADS, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lean_queue<float, 32>, HALO2_THREADS, 0);
+    return e == cudaSuccess ? nb : 0;
+}
+
 // General tiles (an H source in the footprint) and probe blocks of every
 // instance, one launch per step (LeanGen).
 template <typename real, int ZB>
@@ -1481,10 +1533,11 @@ template <typename real>
 cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* d_insts,
                              const InstDev<real>* d_parity, const LeanTiles* tiles, const LeanGroup* groups,
                              int n_groups, const LeanGen& gen, const LeanFix& fix, int n_inst, int zb, int dry,
-                             int cur, DevState* st, const LeanStreams& ls, int one_column) {
+                             int cur, DevState* st, const LeanStreams& ls, int one_column,
+                             const LeanQueue<real>* queue) {
     cudaError_t e = cudaSuccess;
     const bool fork = ls.side[0] != nullptr;
-    const int nsets = fork ? std::min(std::max(n_groups, 1), LEAN_SETS) : 0;
+    const int nsets = fork ? (queue ? 1 : std::min(std::max(n_groups, 1), LEAN_SETS)) : 0;
     if (fork) {
         e = cudaEventRecord(ls.fork, ls.main);
         for (int q = 0; q < nsets * LEAN_CLASSES && e == cudaSuccess; ++q)
@@ -1511,8 +1564,33 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
     auto set_streams = [&](int s, cudaStream_t* sc) {
         for (int c = 0; c < LEAN_CLASSES; ++c) sc[c] = fork ? ls.side[(s % LEAN_SETS) * LEAN_CLASSES + c] : ls.main;
     };
+    // queued: every group's plain, slab and multi tiles in one launch
+    if (queue && queue->n_items) {
+        cudaStream_t sc[LEAN_CLASSES];
+        set_streams(0, sc);
+        const LeanTable<real>* tabs = queue->tabs + (size_t)(dry ? 2 : 0) * queue->n_groups +
+                                      (size_t)cur * queue->n_groups;
+        LeanQueueParams<real> qp;
+        memset(&qp, 0, sizeof(qp));
+        for (int g = 0; g < queue->n_groups && g < LEAN_QUEUE_GROUPS; ++g) qp.t[g] = tabs[g];
+        e = cudaMemsetAsync(queue->ctr, 0, sizeof(unsigned), sc[LEAN_MULTI]);
+        const unsigned grid = (unsigned)std::min<long long>(queue->grid, queue->n_items);
+        if (e == cudaSuccess) {
+            if constexpr (sizeof(real) == 4) {
+                switch (zb) {
+                    case 8: k_lean_queue<real, 8><<<grid, halo2, 0, sc[LEAN_MULTI]>>>(qp, queue->items, queue->n_items, queue->ctr); break;
+                    case 16: k_lean_queue<real, 16><<<grid, halo2, 0, sc[LEAN_MULTI]>>>(qp, queue->items, queue->n_items, queue->ctr); break;
+                    case 32: k_lean_queue<real, 32><<<grid, halo2, 0, sc[LEAN_MULTI]>>>(qp, queue->items, queue->n_items, queue->ctr); break;
+                    default: return cudaErrorInvalidValue;
+                }
+                e = cudaGetLastError();
+            } else {
+                e = cudaErrorInvalidValue;
+            }
+        }
+    }
     // plain, slab and multi tiles: one launch per group and class, blockIdx.y = member
-    for (int g = 0; g < n_groups && e == cudaSuccess; ++g) {
+    for (int g = 0; g < n_groups && e == cudaSuccess && !queue; ++g) {
         LeanTable<real> t = table(groups[g].lead);
         const LeanTiles& T = tiles[groups[g].lead];
         const unsigned gn = (unsigned)groups[g].n;
@@ -1592,9 +1670,9 @@ cudaError_t launch_lean_step(const InstDev<real>* h_insts, const InstDev<real>* 
 template cudaError_t launch_lean_step<double>(const InstDev<double>*, const InstDev<double>*,
                                               const InstDev<double>*, const LeanTiles*, const LeanGroup*, int,
                                               const LeanGen&, const LeanFix&, int, int, int, int, DevState*,
-                                              const LeanStreams&, int);
+                                              const LeanStreams&, int, const LeanQueue<double>*);
 template cudaError_t launch_lean_step<float>(const InstDev<float>*, const InstDev<float>*, const InstDev<float>*,
                                              const LeanTiles*, const LeanGroup*, int, const LeanGen&,
                                              const LeanFix&, int, int, int, int, DevState*, const LeanStreams&,
-                                             int);
+                                             int, const LeanQueue<float>*);
 }  // namespace sj

@@ -83,6 +83,14 @@ class Fields:
         (default), 1 = one column per thread everywhere (same results)."""
         self._ck(self.lib.sj_set_fused_columns(self.handle, int(columns)))
 
+    def set_fused_launch(self, mode):
+        """"grouped" (one launch per group and tile class) or "queue" (one
+        launch of resident blocks claiming every group's tiles)."""
+        self._ck(self.lib.sj_set_fused_launch(self.handle, {"grouped": 0, "queue": 1}[mode]))
+
+    def fused_launch(self):
+        return {0: "grouped", 1: "queue"}[int(self.lib.sj_get_fused_launch(self.handle))]
+
     def tiling(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         self._ck(self.lib.sj_get_tiling(self.handle, C.byref(a), C.byref(b), C.byref(c)))

@@ -335,3 +335,29 @@ def test_snapshot_ring_full_stops_stepping(lib):
     f.set_snapshots(_abi.EZ, every=0)
     f.step(3)
     assert f.snapshots_pending() == 0 and f.steps_done == 8
+
+
+def test_queued_launch_equals_grouped_launches(lib):
+    # FP32 instances with whole 32-column rows (three 64^3 and two 96^3
+    # junctions): one queued launch of resident blocks claiming every
+    # group's tiles gives the same bits as the grouped launches, stepped
+    # directly and through graph replays
+    shapes = [(64, 20.0, 0.3, 2.0), (96, 30.0, 1.1, 0.7), (64, 20.0, 2.9, 0.2), (96, 30.0, 5.0, 3.0),
+              (64, 20.0, 4.4, 1.3)]
+    insts = [junction_instance(n=n, res=r, phase=ph, amplitude=a, probe_components=("Ex", "Ez"))
+             for (n, r, ph, a) in shapes]
+    a = Fields(insts, "f32", "fused")
+    b = Fields(insts, "f32", "fused")
+    b.set_fused_launch("queue")
+    assert b.fused_launch() == "queue" and a.fused_launch() == "grouped"
+    assert b.launches_per_step() < a.launches_per_step()
+    a.step(70)
+    b.step(20)
+    b.step_graph(50, 5)
+    for q in range(len(insts)):
+        for c in range(6):
+            np.testing.assert_array_equal(b.get_array(c, q), a.get_array(c, q), err_msg=f"instance {q} component {c}")
+        np.testing.assert_array_equal(b.monitors(q), a.monitors(q))
+    g = Fields(junction_instance(n=48, res=15.0), "f32", "fused")
+    with pytest.raises(_abi.SJError):          # nx = 48: no whole 32-column rows
+        g.set_fused_launch("queue")
