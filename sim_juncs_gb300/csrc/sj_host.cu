@@ -187,7 +187,8 @@ struct sj_sim {
     std::vector<LeanTable<float>> q_tabs;  // [dry][parity][group] descriptors (host; kernel parameters)
     void* d_qitems = nullptr;
     long long q_version = -1;          // table_version the queue tables were built from
-    int q_zb = -1;                     // z-segment length the queue items were built for
+    long long lists_version = 0;       // bumped whenever prepare_lean rebuilds the tile lists
+    long long q_lists = -1;            // lists_version the queue items were built from
     // dump_raw snapshots (per instance) and the stream their host copies run on
     std::vector<Snapshots> snaps;
     cudaStream_t copy_stream = nullptr;
@@ -1026,6 +1027,7 @@ void prepare_lean(sj_sim* sim) {
     }
     sim->h_tiles = all;
     sim->h_tile_off = off;
+    sim->lists_version += 1;
     sim->dfree(sim->d_tiles);
     sim->d_tiles = sim->upload(all);
     const unsigned* base = reinterpret_cast<const unsigned*>(sim->d_tiles);
@@ -1075,7 +1077,7 @@ const LeanQueue<real>* prepare_queue(sj_sim* sim) {
         return nullptr;
     } else {
         if (sim->l_launch != SJ_LAUNCH_QUEUE || !queue_eligible<real>(sim)) return nullptr;
-        if (sim->q_version == sim->table_version && sim->q_zb == sim->lean_zb) return &sim->queue;
+        if (sim->q_version == sim->table_version && sim->q_lists == sim->lists_version) return &sim->queue;
         const auto& dv = devv<float>(sim);
         const int ng = (int)sim->lgroups.size();
         // [dry][parity][group]
@@ -1095,6 +1097,9 @@ const LeanQueue<real>* prepare_queue(sj_sim* sim) {
                     t.dry = dry;
                     t.qvol = (unsigned)t.inst.vol;
                 }
+        sim->queue.tabs = tabs.data();
+        sim->q_version = sim->table_version;
+        if (sim->q_lists == sim->lists_version) return &sim->queue;  // the items still hold
         // items: multi-slab tiles of every group, then single-slab, then plain;
         // groups of larger grids first, members in order
         std::vector<int> order(ng);
@@ -1120,13 +1125,11 @@ const LeanQueue<real>* prepare_queue(sj_sim* sim) {
         ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
         const int nb = lean_queue_blocks_per_sm(sim->lean_zb);
         if (nb < 1) fail(SJ_E_CUDA, "queued tile kernel cannot be resident");
-        sim->queue.tabs = tabs.data();
         sim->queue.items = reinterpret_cast<const uint4*>(sim->d_qitems);
         sim->queue.n_items = (unsigned)items.size();
         sim->queue.n_groups = ng;
         sim->queue.grid = nb * sms;
-        sim->q_version = sim->table_version;
-        sim->q_zb = sim->lean_zb;
+        sim->q_lists = sim->lists_version;
         return &sim->queue;
     }
 }
