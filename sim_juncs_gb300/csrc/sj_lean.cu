@@ -1424,6 +1424,9 @@ k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
                 const real e_old = I.F[cur][c][o];
                 real corr = 0;
                 for (int p = 0; p < I.n_poles; ++p) {
+                    // a pole the material does not have at this E point keeps
+                    // P = 0 and adds +0: it is neither read nor written
+                    if (cf[3 + 3 * p + c] == real(0)) continue;
                     real* pp = I.P + ((long long)(p * 2 + 0) * 3 + c) * I.dvol + di;
                     real* pm = I.P + ((long long)(p * 2 + 1) * 3 + c) * I.dvol + di;
                     const real pn = *pp, pq = *pm;

@@ -117,6 +117,7 @@ __device__ __forceinline__ real e_finish(const InstDev<real>& I, int i, int j, i
         const long long di =
             ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]);
         for (int p = 0; p < I.n_poles; ++p) {
+            if (cf[3 + 3 * p + CA] == real(0)) continue;  // P stays 0: acc - (+0) = acc
             real* pp = I.P + ((long long)(p * 2 + 0) * 3 + CA) * I.dvol + di;
             real* pm = I.P + ((long long)(p * 2 + 1) * 3 + CA) * I.dvol + di;
             const real pn = *pp, pq = *pm;
@@ -156,6 +157,7 @@ __device__ __forceinline__ real e_finish_row(const InstDev<real>& I, int i, int 
         const long long di =
             ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]);
         for (int p = 0; p < I.n_poles; ++p) {
+            if (cf[3 + 3 * p + CA] == real(0)) continue;  // P stays 0: acc - (+0) = acc
             real* pp = I.P + ((long long)(p * 2 + 0) * 3 + CA) * I.dvol + di;
             real* pm = I.P + ((long long)(p * 2 + 1) * 3 + CA) * I.dvol + di;
             const real pn = *pp, pq = *pm;
