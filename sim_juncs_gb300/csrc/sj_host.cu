@@ -587,6 +587,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
     I.ncoef = 6 + 3 * np;
     std::vector<real> coef((size_t)nk * I.ncoef);
     std::vector<uint8_t> cflag(nk, 0);
+    std::vector<uint32_t> pmask(nk, 0);
     for (int q = 0; q < nk; ++q) {
         for (int c = 0; c < 3; ++c) {
             const int cl = (H.keys[q] >> (8 * c)) & 255;
@@ -595,6 +596,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
                 const double cs = Cp[p] * sigma[(size_t)cl * np + p];
                 coef[(size_t)q * I.ncoef + 3 + 3 * p + c] = (real)cs;
                 if (cs != 0.0) cflag[q] |= 1;
+                if ((real)cs != real(0)) pmask[q] |= 1u << (8 * c + p);
             }
             // S eps_inf^-1, the product the fused E update scales curl H by
             // (a product of two `real`s: the bits of the device's I.S * inv)
@@ -603,6 +605,7 @@ void build_instance(sj_sim* sim, const sj_instance_desc& d, HostInst<real>& H, I
     }
     I.coef = sim->upload(coef);
     I.cflag = sim->upload(cflag);
+    I.pmask = sim->upload(pmask);
     H.coef = coef;
 
     // ---- dispersive bounding box and polarisation storage

@@ -50,6 +50,7 @@ struct InstDev {
     const uint8_t* combo;       // [nz][ny][px]
     const real* coef;           // [n_combos][ncoef]: inv_eps[3], Csig[p][3], then S * inv_eps[3]
     const uint8_t* cflag;       // [n_combos]: bit 0 = some pole has sigma != 0
+    const uint32_t* pmask;      // [n_combos]: bit 8 c + p = pole p has C sigma != 0 at E component c
     int n_combos, ncoef;
     int n_poles;
     real A[MAXP], B[MAXP];

@@ -1402,47 +1402,102 @@ k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
 }
 
 // meep's Lorentz/Drude ADE over the dispersive bounding box:
-// P^{n+1} = A P^n + B P^{n-1} + C sigma E^n per pole, and
-// E^{n+1} = fma(-eps_inf^{-1}, sum_p (P^{n+1} - P^n), E^{n+1})
+// P^{n+1} = A P^n + B P^{n-1} + C sigma E^n per pole the material has at the
+// E point (pmask), and E^{n+1} = fma(-eps_inf^{-1}, sum_p (P^{n+1} - P^n),
+// E^{n+1}).  A pole the material does not have at the E point keeps P = 0
+// and would add +0: it is neither read nor written, and neither is a
+// component without poles.  One thread per voxel (its three components), a
+// block per DISP_VOXELS voxels of the box (DISP_R per thread, in turn): per
+// voxel the combo first, then E and P of the first two poles of every
+// component together (a third and later pole of a component, which no
+// material here has, follows in order).
+constexpr int DISP_R = 4;
+constexpr int DISP_VOXELS = DISP_R * FIX_THREADS;
 template <typename real>
-__global__ void __launch_bounds__(FIX_THREADS)
+__global__ void __launch_bounds__(FIX_THREADS, sizeof(real) == 4 ? 3 : 2)
 k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int cur, unsigned step_blocks,
             int dry, DevState* st) {
     const long long n = st->step;
     const int2 e = __ldg(blk + blockIdx.x);
     const InstDev<real>& I = insts[e.x];
-    const long long di = (long long)e.y * FIX_THREADS + threadIdx.x;
-    if (di < I.dvol) {
-        const int i = I.dlo[0] + (int)(di % I.dn[0]);
-        const int j = I.dlo[1] + (int)((di / I.dn[0]) % I.dn[1]);
-        const int k = I.dlo[2] + (int)(di / ((long long)I.dn[0] * I.dn[1]));
-        const long long o = (long long)k * I.plane + (long long)j * I.px + i;
-        const int cb = I.combo[o];
-        if (I.cflag[cb] & 1) {
-            const real* cf = I.coef + cb * I.ncoef;
-            for (int c = 0; c < 3; ++c) {
-                const real e_old = I.F[cur][c][o];
-                real corr = 0;
-                for (int p = 0; p < I.n_poles; ++p) {
-                    // a pole the material does not have at this E point keeps
-                    // P = 0 and adds +0: it is neither read nor written
-                    if (cf[3 + 3 * p + c] == real(0)) continue;
-                    real* pp = I.P + ((long long)(p * 2 + 0) * 3 + c) * I.dvol + di;
-                    real* pm = I.P + ((long long)(p * 2 + 1) * 3 + c) * I.dvol + di;
-                    const real pn = *pp, pq = *pm;
-                    const real pnew = I.A[p] * pn + I.B[p] * pq + cf[3 + 3 * p + c] * e_old;
-                    corr += pnew - pn;
-                    if (!dry) {
-                        *pm = pn;
-                        *pp = pnew;
-                    }
+    // the descriptor's fields, read once (offsets within an instance fit 32 bits)
+    const unsigned dvol = (unsigned)I.dvol, d0 = (unsigned)I.dn[0], d1 = (unsigned)I.dn[1];
+    const int lo0 = I.dlo[0], lo1 = I.dlo[1], lo2 = I.dlo[2];
+    const unsigned plane = (unsigned)I.plane, px = (unsigned)I.px;
+    const uint8_t* combo = I.combo;
+    const uint32_t* pmask = I.pmask;
+    const real* coef = I.coef;
+    const int ncoef = I.ncoef;
+    real* const P = I.P;
+    const real* Eo[3] = {I.F[cur][0], I.F[cur][1], I.F[cur][2]};
+    real* const En[3] = {I.F[cur ^ 1][0], I.F[cur ^ 1][1], I.F[cur ^ 1][2]};
+    const long long lv = 3 * (long long)dvol;  // from level n to level n-1 of a pole
+    const unsigned base = (unsigned)e.y * DISP_VOXELS + threadIdx.x;
+    for (int r = 0; r < DISP_R; ++r) {
+        const unsigned u = base + r * FIX_THREADS;
+        if (u >= dvol) break;
+        const unsigned q = u / d0, kk = q / d1;
+        const int i = lo0 + (int)(u - q * d0), j = lo1 + (int)(q - kk * d1), k = lo2 + (int)kk;
+        const unsigned o = (unsigned)k * plane + (unsigned)j * px + (unsigned)i;
+        const int cb = combo[o];
+        const unsigned mask = pmask[cb];
+        if (!mask) continue;
+        const real* cf = coef + cb * ncoef;
+        real eo[3], ec[3], pn1[3], pq1[3], pn2[3], pq2[3], c1[3], c2[3];
+        int pa[3], pb[3];
+        unsigned rest[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const unsigned m = (mask >> (8 * c)) & 255u;
+            const unsigned m2 = m & (m - 1);
+            pa[c] = m ? __ffs(m) - 1 : -1;
+            pb[c] = m2 ? __ffs(m2) - 1 : -1;
+            rest[c] = m2 & (m2 - 1);
+            eo[c] = m ? Eo[c][o] : real(0);
+            ec[c] = m ? En[c][o] : real(0);
+            const long long a1 = ((long long)pa[c] * 6 + c) * dvol + u, a2 = ((long long)pb[c] * 6 + c) * dvol + u;
+            c1[c] = m ? cf[3 + 3 * pa[c] + c] : real(0);
+            c2[c] = m2 ? cf[3 + 3 * pb[c] + c] : real(0);
+            pn1[c] = m ? P[a1] : real(0), pq1[c] = m ? P[a1 + lv] : real(0);
+            pn2[c] = m2 ? P[a2] : real(0), pq2[c] = m2 ? P[a2 + lv] : real(0);
+        }
+        const long long d = design_index(I, i, j, k);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (pa[c] < 0) continue;
+            real corr = 0;
+            {
+                const real pnew = I.A[pa[c]] * pn1[c] + I.B[pa[c]] * pq1[c] + c1[c] * eo[c];
+                corr += pnew - pn1[c];
+                if (!dry) {
+                    real* pp = P + ((long long)pa[c] * 6 + c) * dvol + u;
+                    pp[lv] = pn1[c];
+                    *pp = pnew;
                 }
-                real* E = I.F[cur ^ 1][c];
-                const long long d = design_index(I, i, j, k);
-                E[o] = fma(-(d >= 0 ? I.dinv[d] : cf[c]), corr, E[o]);
-                if (!dry)
-                    if (real* r = design_rec(I, d, n, c)) *r -= corr;
             }
+            if (pb[c] >= 0) {
+                const real pnew = I.A[pb[c]] * pn2[c] + I.B[pb[c]] * pq2[c] + c2[c] * eo[c];
+                corr += pnew - pn2[c];
+                if (!dry) {
+                    real* pp = P + ((long long)pb[c] * 6 + c) * dvol + u;
+                    pp[lv] = pn2[c];
+                    *pp = pnew;
+                }
+            }
+            for (unsigned m = rest[c]; m; m &= m - 1) {
+                const int p = __ffs(m) - 1;
+                real* pp = P + ((long long)p * 6 + c) * dvol + u;
+                const real pn = *pp, pq = pp[lv];
+                const real pnew = I.A[p] * pn + I.B[p] * pq + cf[3 + 3 * p + c] * eo[c];
+                corr += pnew - pn;
+                if (!dry) {
+                    pp[lv] = pn;
+                    *pp = pnew;
+                }
+            }
+            En[c][o] = fma(-(d >= 0 ? I.dinv[d] : cf[c]), corr, ec[c]);
+            if (!dry)
+                if (real* rr = design_rec(I, d, n, c)) *rr -= corr;
         }
     }
     finish_block(step_blocks, dry, st);
@@ -1522,7 +1577,7 @@ void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>
             for (long long b = 0; b * FIX_THREADS < cells; ++b) passes[s].push_back(make_int2(q, (int)b));
         }
         if (I.n_poles > 0 && I.dvol > 0)
-            for (long long b = 0; b * FIX_THREADS < I.dvol; ++b)
+            for (long long b = 0; b * DISP_VOXELS < I.dvol; ++b)
                 passes[SJ_MAX_SOURCES].push_back(make_int2(q, (int)b));
     }
 }

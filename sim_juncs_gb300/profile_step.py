@@ -6,7 +6,9 @@
 Workloads: sweep (32 x 96^3 + 32 x 128^3 + 32 x 192^3 junctions),
 junction192 (one 192^3 sweep member), junction192x4 (four 192^3 sweep
 members: one launch group, ~3.4 GB on the device), bowtie (512 x 512 x
-384), junction64 (64^3).  Prints the launches per step so that a capture
+384), junction64 (64^3), inverseN (the first N of the 16 inverse-design
+instances at 192^3: Au on a quartz substrate, each with its design region;
+~1.1 GB each).  Prints the launches per step so that a capture
 can skip set-up launches and warm-up steps by count.
 
 --diag energy: after the steps, three sj_energy calls (k_energy + k_sum);
@@ -31,7 +33,16 @@ def instances(name):
         return [configs.bowtie_instance()]
     if name == "junction64":
         return [configs.junction_instance()]
+    if name.startswith("inverse"):
+        return [configs.inverse_design_case(d)[0] for d in range(int(name[7:]))]
     raise SystemExit(f"unknown workload {name!r}")
+
+
+def designs(name):
+    """The design regions a workload's instances carry (instance, Design)."""
+    if name.startswith("inverse"):
+        return [(d, configs.inverse_design_case(d)[1]) for d in range(int(name[7:]))]
+    return []
 
 
 def main():
@@ -44,6 +55,8 @@ def main():
     p.add_argument("--diag", default=None, choices=["energy", "phases"])
     a = p.parse_args()
     f = Fields(instances(a.workload), a.precision, a.schedule)
+    for q, des in designs(a.workload):
+        f.set_design(des, q)
     if f.schedule_name() == "fused":
         f.set_tiling(8, 0, a.zseg)
     f.step(a.steps)
