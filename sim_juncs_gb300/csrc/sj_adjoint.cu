@@ -46,7 +46,10 @@ __device__ __forceinline__ long long design_index(const InstDev<real>& I, int i,
 }
 
 // Transpose of the E update at one voxel (three components).  eb holds
-// dF/dE^{n+1} on entry and the E update's share of dF/dE^n on exit.
+// dF/dE^{n+1} on entry and the E update's share of dF/dE^n on exit.  Every
+// load of the voxel goes out first (eb, the E-side psi adjoints of its slab
+// axes, the polarisation adjoints of the poles its material has: pmask),
+// then the three components are formed in turn.
 template <typename real>
 __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDev<real> A, long long n) {
     const InstDev<real>& I = A.I;
@@ -56,45 +59,71 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDe
     const int idx[3] = {i, j, k};
     const int cb = I.combo[o];
     const real* cf = I.coef + cb * I.ncoef;
-    const bool disp = (I.cflag[cb] & 1) != 0;
+    const unsigned mask = I.pmask[cb];
     const long long di =
-        disp ? ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]) : 0;
+        mask ? ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]) : 0;
     const long long d = design_index(I, i, j, k);
     const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
+    const bool sl[3] = {in_slab(I, 0, i), in_slab(I, 1, j), in_slab(I, 2, k)};
+    real ebo[3], q1[3], q2[3], b0[3], b1[3], c0[3], c1[3];
+    int pa[3], pz[3];
+    real pa0[3], pa1[3], pz0[3], pz1[3];
+    unsigned rest[3];
+#pragma unroll
+    for (int ca = 0; ca < 3; ++ca) {
+        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+        const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
+        ebo[ca] = A.eb[ca][o];
+        q1[ca] = sl[a1] ? A.psEb[a1][(long long)s1 * I.vol + o] : real(0);
+        q2[ca] = sl[a2] ? A.psEb[a2][(long long)s2 * I.vol + o] : real(0);
+        b0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 0) : real(0), c0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 1) : real(0);
+        b1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 0) : real(0), c1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 1) : real(0);
+        const unsigned m = (mask >> (8 * ca)) & 255u, m2 = m & (m - 1);
+        pa[ca] = m ? __ffs(m) - 1 : -1;
+        pz[ca] = m2 ? __ffs(m2) - 1 : -1;
+        rest[ca] = m2 & (m2 - 1);
+        const long long x0 = ((long long)(pa[ca] * 2) * 3 + ca) * I.dvol + di;
+        const long long x1 = ((long long)(pz[ca] * 2) * 3 + ca) * I.dvol + di;
+        pa0[ca] = m ? A.pb[x0] : real(0), pa1[ca] = m ? A.pb[x0 + 3 * I.dvol] : real(0);
+        pz0[ca] = m2 ? A.pb[x1] : real(0), pz1[ca] = m2 ? A.pb[x1 + 3 * I.dvol] : real(0);
+    }
+#pragma unroll
     for (int ca = 0; ca < 3; ++ca) {
         const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
         const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
         const real inv = d >= 0 ? I.dinv[d] : cf[ca];
-        const real ebo = A.eb[ca][o];
-        if (d >= 0) A.g[d * 3 + ca] += (double)ebo * (double)A.rec[((n - A.rec_t0) * nd + d) * 3 + ca];
-        const real ab = inv * ebo;  // adjoint of the bracket acc
-        real ein = ebo;
-        if (disp)
-            for (int p = 0; p < I.n_poles; ++p) {
-                const real cs = cf[3 + 3 * p + ca];
-                if (cs == real(0)) continue;  // P is never excited there and does not reach E
-                real* p0 = A.pb + ((long long)(p * 2 + 0) * 3 + ca) * I.dvol + di;
-                real* p1 = A.pb + ((long long)(p * 2 + 1) * 3 + ca) * I.dvol + di;
-                const real pnb = *p0 - ab;                    // dF/dP^{n+1}
-                const real pn = *p1 + ab + I.A[p] * pnb;      // dF/dP^n
-                *p1 = I.B[p] * pnb;                           // dF/dP^{n-1}
-                *p0 = pn;
-                ein += cs * pnb;
-            }
+        if (d >= 0) A.g[d * 3 + ca] += (double)ebo[ca] * (double)A.rec[((n - A.rec_t0) * nd + d) * 3 + ca];
+        const real ab = inv * ebo[ca];  // adjoint of the bracket acc
+        real ein = ebo[ca];
+        // one pole's ADE transpose: (dF/dP^{n+1}, dF/dP^n) -> (dF/dP^n, dF/dP^{n-1})
+        auto pole = [&](int p, real q0v, real q1v) {
+            real* p0 = A.pb + ((long long)(p * 2 + 0) * 3 + ca) * I.dvol + di;
+            real* p1 = A.pb + ((long long)(p * 2 + 1) * 3 + ca) * I.dvol + di;
+            const real pnb = q0v - ab;                    // dF/dP^{n+1}
+            const real pn = q1v + ab + I.A[p] * pnb;      // dF/dP^n
+            *p1 = I.B[p] * pnb;                           // dF/dP^{n-1}
+            *p0 = pn;
+            ein += cf[3 + 3 * p + ca] * pnb;
+        };
+        if (pa[ca] >= 0) pole(pa[ca], pa0[ca], pa1[ca]);
+        if (pz[ca] >= 0) pole(pz[ca], pz0[ca], pz1[ca]);
+        for (unsigned m = rest[ca]; m; m &= m - 1) {
+            const int p = __ffs(m) - 1;
+            const long long x = ((long long)(p * 2) * 3 + ca) * I.dvol + di;
+            pole(p, A.pb[x], A.pb[x + 3 * I.dvol]);
+        }
         A.eb[ca][o] = ein;
         const real cv = I.S * ab;  // adjoint of the curl
         real t1 = cv, t2 = -cv;
-        if (in_slab(I, a1, idx[a1])) {
-            real* ps = A.psEb[a1] + (long long)s1 * I.vol + o;
-            const real t = *ps + cv;
-            t1 = cv + prof_at(I, a1, idx[a1], 1) * t;
-            *ps = prof_at(I, a1, idx[a1], 0) * t;
+        if (sl[a1]) {
+            const real t = q1[ca] + cv;
+            t1 = cv + c0[ca] * t;
+            A.psEb[a1][(long long)s1 * I.vol + o] = b0[ca] * t;
         }
-        if (in_slab(I, a2, idx[a2])) {
-            real* ps = A.psEb[a2] + (long long)s2 * I.vol + o;
-            const real t = *ps - cv;
-            t2 = -cv + prof_at(I, a2, idx[a2], 1) * t;
-            *ps = prof_at(I, a2, idx[a2], 0) * t;
+        if (sl[a2]) {
+            const real t = q2[ca] - cv;
+            t2 = -cv + c1[ca] * t;
+            A.psEb[a2][(long long)s2 * I.vol + o] = b1[ca] * t;
         }
         A.t1[ca][o] = t1;  // adjoint of H_a2(o) - H_a2(o - e_a1)
         A.t2[ca][o] = t2;  // adjoint of H_a1(o) - H_a1(o - e_a2)

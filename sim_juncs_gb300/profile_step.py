@@ -11,6 +11,9 @@ instances at 192^3: Au on a quartz substrate, each with its design region;
 ~1.1 GB each).  Prints the launches per step so that a capture
 can skip set-up launches and warm-up steps by count.
 
+--adjoint: instead of plain steps, one sj_adjoint_gradient over N steps
+(inverseN: every instance's own objective; one checkpoint segment), so the
+forward, re-run and adjoint kernels are captured;
 --diag energy: after the steps, three sj_energy calls (k_energy + k_sum);
 --diag phases: then the phases of 384 monitor series (the sweep's 96 x 4
 gap points, here 48 copies of the 64^3 junction's 8) in one sj_extract_phases
@@ -38,6 +41,13 @@ def instances(name):
     raise SystemExit(f"unknown workload {name!r}")
 
 
+def objectives(name):
+    """The objectives of a workload's instances (inverseN only)."""
+    if name.startswith("inverse"):
+        return [configs.inverse_design_case(d)[2] for d in range(int(name[7:]))]
+    raise SystemExit(f"{name!r} has no objectives")
+
+
 def designs(name):
     """The design regions a workload's instances carry (instance, Design)."""
     if name.startswith("inverse"):
@@ -53,13 +63,17 @@ def main():
     p.add_argument("--zseg", type=int, default=8)
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--diag", default=None, choices=["energy", "phases"])
+    p.add_argument("--adjoint", action="store_true")
     a = p.parse_args()
     f = Fields(instances(a.workload), a.precision, a.schedule)
     for q, des in designs(a.workload):
         f.set_design(des, q)
     if f.schedule_name() == "fused":
         f.set_tiling(8, 0, a.zseg)
-    f.step(a.steps)
+    if a.adjoint:
+        f.adjoint_gradient(objectives(a.workload), a.steps, a.steps)
+    else:
+        f.step(a.steps)
     f.synchronize()
     print(f"{a.workload} {a.precision} {f.schedule_name()} steps={f.steps_done} voxels={f.voxels()} "
           f"launches_per_step={f.launches_per_step()}", flush=True)
