@@ -1410,11 +1410,21 @@ k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
 // block per DISP_VOXELS voxels of the box (DISP_R per thread, in turn): per
 // voxel the combo first, then E and P of the first two poles of every
 // component together (a third and later pole of a component, which no
-// material here has, follows in order).
-constexpr int DISP_R = 4;
+// material here has, follows in order).  Sixteen voxels per thread and four
+// blocks per SM (64 registers): every block ends with the step counter's
+// fence and atomic, so fewer, longer blocks pay less for it (16 x 192^3 Au on
+// quartz, forward step: 4 voxels, 3 blocks per SM 3.21 ms; 4, 4: 2.99; 8, 4:
+// 2.89; 16, 4: 2.85; 32, 4: 2.85).
+#ifndef SJ_DISP_R
+#define SJ_DISP_R 16
+#endif
+#ifndef SJ_DISP_MINB
+#define SJ_DISP_MINB 4
+#endif
+constexpr int DISP_R = SJ_DISP_R;
 constexpr int DISP_VOXELS = DISP_R * FIX_THREADS;
 template <typename real>
-__global__ void __launch_bounds__(FIX_THREADS, sizeof(real) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(FIX_THREADS, sizeof(real) == 4 ? SJ_DISP_MINB : 2)
 k_lean_disp(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int cur, unsigned step_blocks,
             int dry, DevState* st) {
     const long long n = st->step;
