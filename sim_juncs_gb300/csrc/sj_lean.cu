@@ -1377,6 +1377,11 @@ k_lean_general(const InstDev<real>* __restrict__ parity_tab, const int4* __restr
 // device table; `cur` is the step's parity.
 
 // E^{n+1} = fma(-eps_inf^{-1}, dt J_s, E^{n+1}) over source s's box
+// ESRC_R cells of the box per thread, in turn (fewer, longer blocks pay
+// less for the step counter's fence and atomic at the end of each block);
+// box coordinates in 32 bits.
+constexpr int ESRC_R = 8;
+constexpr int ESRC_CELLS = ESRC_R * FIX_THREADS;
 template <typename real>
 __global__ void __launch_bounds__(FIX_THREADS)
 k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ blk, int slot, int cur,
@@ -1385,18 +1390,23 @@ k_lean_esrc(const InstDev<real>* __restrict__ insts, const int2* __restrict__ bl
     const int2 e = __ldg(blk + blockIdx.x);
     const InstDev<real>& I = insts[e.x];
     const SrcDev<real>& sv = I.src[slot];
-    const long long cell = (long long)e.y * FIX_THREADS + threadIdx.x;
-    const long long n01 = (long long)sv.n[0] * sv.n[1];
-    if (cell < n01 * sv.n[2]) {
-        const int di = (int)(cell % sv.n[0]), dj = (int)((cell / sv.n[0]) % sv.n[1]), dk = (int)(cell / n01);
-        const long long o = (long long)(sv.lo[2] + dk) * I.plane + (long long)(sv.lo[1] + dj) * I.px + (sv.lo[0] + di);
-        real* E = I.F[cur ^ 1][sv.comp];
-        const long long d = design_index(I, sv.lo[0] + di, sv.lo[1] + dj, sv.lo[2] + dk);
-        const real cfc = d >= 0 ? I.dinv[d] : I.coef[(int)I.combo[o] * I.ncoef + sv.comp];
-        const real J = (real)sv.tab[n] * sv.w[0][di] * sv.w[1][dj] * sv.w[2][dk];
+    const unsigned n0 = (unsigned)sv.n[0], n1 = (unsigned)sv.n[1];
+    const unsigned cells = n0 * n1 * (unsigned)sv.n[2];
+    const int lo0 = sv.lo[0], lo1 = sv.lo[1], lo2 = sv.lo[2], comp = sv.comp;
+    const real tn = (real)sv.tab[n];
+    real* const E = I.F[cur ^ 1][comp];
+    for (int r = 0; r < ESRC_R; ++r) {
+        const unsigned cell = (unsigned)e.y * ESRC_CELLS + r * FIX_THREADS + threadIdx.x;
+        if (cell >= cells) break;
+        const unsigned q = cell / n0, dk = q / n1;
+        const int di = (int)(cell - q * n0), dj = (int)(q - dk * n1);
+        const long long o = (long long)(lo2 + (int)dk) * I.plane + (long long)(lo1 + dj) * I.px + (lo0 + di);
+        const long long d = design_index(I, lo0 + di, lo1 + dj, lo2 + (int)dk);
+        const real cfc = d >= 0 ? I.dinv[d] : I.coef[(int)I.combo[o] * I.ncoef + comp];
+        const real J = tn * sv.w[0][di] * sv.w[1][dj] * sv.w[2][dk];
         E[o] = fma(-cfc, J, E[o]);
         if (!dry)
-            if (real* r = design_rec(I, d, n, sv.comp)) *r -= J;
+            if (real* rr = design_rec(I, d, n, comp)) *rr -= J;
     }
     finish_block(step_blocks, dry, st);
 }
@@ -1584,7 +1594,7 @@ void lean_fix_blocks(const InstDev<real>* h_insts, int n_inst, std::vector<int2>
         for (int s = 0; s < I.n_src; ++s) {
             if (I.src[s].comp >= 3) continue;
             const long long cells = (long long)I.src[s].n[0] * I.src[s].n[1] * I.src[s].n[2];
-            for (long long b = 0; b * FIX_THREADS < cells; ++b) passes[s].push_back(make_int2(q, (int)b));
+            for (long long b = 0; b * ESRC_CELLS < cells; ++b) passes[s].push_back(make_int2(q, (int)b));
         }
         if (I.n_poles > 0 && I.dvol > 0)
             for (long long b = 0; b * DISP_VOXELS < I.dvol; ++b)
