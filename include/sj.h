@@ -266,9 +266,10 @@ const char* sj_last_error(const sj_sim* sim);
    (src/disp.cpp:557-645): builds one instance on the current device. */
 int sj_create(const sj_instance_desc* inst, int32_t precision, sj_sim** out);
 
-/* many independent instances stepped by one launch per step (batched
-   CEP/amplitude sweeps); instance i keeps its own grid, materials, PML,
-   sources and probes. */
+/* many independent instances stepped together (batched CEP/amplitude
+   sweeps): instances with equal grid, CPML and materials share every tile
+   launch of a step; instance i keeps its own grid, materials, PML, sources
+   and probes. */
 int sj_batch_create(int32_t n_instances, const sj_instance_desc* insts,
                     int32_t precision, sj_sim** out);
 
