@@ -214,6 +214,8 @@ def run_ours(args):
     if til is not None:
         cfg = dict(cfg, tile=f"32x{til[0]}", tma_ring=til[1], zseg=til[2], tiling="autotuned",
                    autotune_dry_ms_per_step=tune_ms)  # the tuner's launches load but do not store
+        if schedule == "fused":
+            cfg["launch_mode"] = f.fused_launch()  # grouped launches or one queued launch, as the tuner kept
     voxels = f.voxels()
     bytes_step = f.bytes_per_step()
 
