@@ -2,7 +2,8 @@
 
 Workload (default "sweep"): the batched CEP/amplitude sweep — 96 junction
 instances on uneven grids (32 x 96^3, 32 x 128^3, 32 x 192^3), FP32 fields,
-one launch per time step over all instances.  A bench step is one FDTD time
+the instances of one grid size sharing every tile launch (12 launches per
+step, replayed from CUDA graphs).  A bench step is one FDTD time
 step of the whole batch.  The metric is voxel-steps/s = sum of instance
 voxels x steps / device time.  Also reported: the plain FP64 path on a grid
 whose state is well above L2 (512 x 512 x 384), its roofline fraction, and
