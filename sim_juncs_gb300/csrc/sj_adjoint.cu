@@ -10,8 +10,14 @@
 // two cells it reads: a kernel writes the per-cell adjoints of both
 // differences (t1, t2 for the E update, t3, t4 for the H update) and the
 // next gathers them, one thread per cell, so no two threads write one value.
-// Three passes per step: k_adj_e, k_adj_e_gather_h (the gather into dF/dH
-// and, at the same cell, the H update's transpose), k_adj_h_gather.  The
+// Per step: k_adj_e (the E update's transpose), then k_adj_e_gather_h (the
+// gather into dF/dH and, at the same cell, the H update's transpose).  The
+// gather of the H update's differences into dF/dE^n needs every cell's t3,
+// t4 of step n, so it runs at the start of step n-1's k_adj_e, which reads
+// the same cell's eb next (k_adj_e<GATHER>): a step is two launches.  The
+// objective's dF/dE^n source, added to eb between the steps, then precedes
+// that gather instead of following it (the same sum in another order), and
+// the last step's gather, whose dF/dE^0 nothing reads, is never run.  The
 // gradient with respect to a design voxel's inverse eps is
 // sum_n dF/dE^{n+1} * acc^n, acc^n being the E update's bracket at step n,
 // recorded while the segment is re-run forward.
@@ -46,12 +52,17 @@ __device__ __forceinline__ long long design_index(const InstDev<real>& I, int i,
 }
 
 // Transpose of the E update at one voxel (three components).  eb holds
-// dF/dE^{n+1} on entry and the E update's share of dF/dE^n on exit.  Every
-// load of the voxel goes out first (eb, the E-side psi adjoints of its slab
-// axes, the polarisation adjoints of the poles its material has: pmask),
-// then the three components are formed in turn.
-template <typename real>
-__global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDev<real> A, long long n) {
+// dF/dE^{n+1} on entry and the E update's share of dF/dE^n on exit; with
+// GATHER, eb first completes dF/dE^{n+1} with what the H update's
+// differences of step n+1 read from E here (t3, t4 of this cell and of its
+// -1 neighbours).  Every load of the voxel goes out first (eb, t3 and t4, the E-side
+// psi adjoints of its slab axes, the polarisation adjoints of the poles its
+// material has: pmask), then the three components are formed in turn.
+#ifndef SJ_ADJ_E_MINB
+#define SJ_ADJ_E_MINB 3
+#endif
+template <typename real, bool GATHER>
+__global__ void __launch_bounds__(AX * AY, SJ_ADJ_E_MINB) k_adj_e(const __grid_constant__ AdjDev<real> A, long long n) {
     const InstDev<real>& I = A.I;
     const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
     if (i >= I.nx || j >= I.ny) return;
@@ -66,6 +77,7 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDe
     const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
     const bool sl[3] = {in_slab(I, 0, i), in_slab(I, 1, j), in_slab(I, 2, k)};
     real ebo[3], q1[3], q2[3], b0[3], b1[3], c0[3], c1[3];
+    real g3[3], g4[3], m3[3], m4[3];  // GATHER: t3, t4 here and at the -1 neighbours
     int pa[3], pz[3];
     real pa0[3], pa1[3], pz0[3], pz1[3];
     unsigned rest[3];
@@ -78,6 +90,11 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDe
         q2[ca] = sl[a2] ? A.psEb[a2][(long long)s2 * I.vol + o] : real(0);
         b0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 0) : real(0), c0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 1) : real(0);
         b1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 0) : real(0), c1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 1) : real(0);
+        if (GATHER) {
+            g3[ca] = A.t3[ca][o], g4[ca] = A.t4[ca][o];
+            m3[ca] = idx[a1] > 0 ? A.t3[ca][o - stride_of(I, a1)] : real(0);
+            m4[ca] = idx[a2] > 0 ? A.t4[ca][o - stride_of(I, a2)] : real(0);
+        }
         const unsigned m = (mask >> (8 * ca)) & 255u, m2 = m & (m - 1);
         pa[ca] = m ? __ffs(m) - 1 : -1;
         pz[ca] = m2 ? __ffs(m2) - 1 : -1;
@@ -86,6 +103,19 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e(const __grid_constant__ AdjDe
         const long long x1 = ((long long)(pz[ca] * 2) * 3 + ca) * I.dvol + di;
         pa0[ca] = m ? A.pb[x0] : real(0), pa1[ca] = m ? A.pb[x0 + 3 * I.dvol] : real(0);
         pz0[ca] = m2 ? A.pb[x1] : real(0), pz1[ca] = m2 ? A.pb[x1 + 3 * I.dvol] : real(0);
+    }
+    if (GATHER) {
+        // dF/dE^{n+1} += what the H update's differences of step n+1 read here
+#pragma unroll
+        for (int ca = 0; ca < 3; ++ca) {
+            const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
+            real v = -g3[ca];
+            if (idx[a1] > 0) v += m3[ca];
+            ebo[a2] += v;
+            real w = -g4[ca];
+            if (idx[a2] > 0) w += m4[ca];
+            ebo[a1] += w;
+        }
     }
 #pragma unroll
     for (int ca = 0; ca < 3; ++ca) {
@@ -174,25 +204,6 @@ __global__ void __launch_bounds__(AX * AY) k_adj_e_gather_h(const __grid_constan
     }
 }
 
-// dF/dE^n += what the H update's differences read from E at this cell.
-template <typename real>
-__global__ void __launch_bounds__(AX * AY) k_adj_h_gather(const __grid_constant__ AdjDev<real> A) {
-    const InstDev<real>& I = A.I;
-    const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
-    if (i >= I.nx || j >= I.ny) return;
-    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
-    const int idx[3] = {i, j, k};
-    for (int ca = 0; ca < 3; ++ca) {
-        const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
-        real v = -A.t3[ca][o];
-        if (idx[a1] > 0) v += A.t3[ca][o - stride_of(I, a1)];
-        A.eb[a2][o] += v;
-        real w = -A.t4[ca][o];
-        if (idx[a2] > 0) w += A.t4[ca][o - stride_of(I, a2)];
-        A.eb[a1][o] += w;
-    }
-}
-
 // One thread per (objective cell, E component in the mask).
 template <typename real>
 __global__ void k_objective(const __grid_constant__ InstDev<real> I, int cur, const int* __restrict__ cells,
@@ -220,13 +231,16 @@ __global__ void k_objective(const __grid_constant__ InstDev<real> I, int cur, co
 }  // namespace
 
 template <typename real>
-cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, cudaStream_t s) {
+cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, bool first, cudaStream_t s) {
     const dim3 block(AX, AY), grid((a.I.nx + AX - 1) / AX, (a.I.ny + AY - 1) / AY, a.I.nz);
-    k_adj_e<real><<<grid, block, 0, s>>>(a, n);
+    if (first)
+        k_adj_e<real, false><<<grid, block, 0, s>>>(a, n);
+    else
+        k_adj_e<real, true><<<grid, block, 0, s>>>(a, n);
     k_adj_e_gather_h<real><<<grid, block, 0, s>>>(a);
-    k_adj_h_gather<real><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
 }
+
 
 template <typename real>
 cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells, int n_cells, int comp_mask,
@@ -239,8 +253,8 @@ cudaError_t launch_objective(const InstDev<real>& I, int cur, const int* d_cells
     return cudaGetLastError();
 }
 
-template cudaError_t launch_adjoint_step<float>(const AdjDev<float>&, long long, cudaStream_t);
-template cudaError_t launch_adjoint_step<double>(const AdjDev<double>&, long long, cudaStream_t);
+template cudaError_t launch_adjoint_step<float>(const AdjDev<float>&, long long, bool, cudaStream_t);
+template cudaError_t launch_adjoint_step<double>(const AdjDev<double>&, long long, bool, cudaStream_t);
 template cudaError_t launch_objective<float>(const InstDev<float>&, int, const int*, int, int, double, double2*,
                                              long long, bool, float* const*, cudaStream_t);
 template cudaError_t launch_objective<double>(const InstDev<double>&, int, const int*, int, int, double, double2*,

@@ -1701,6 +1701,7 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
     }
     // ---- backwards, one segment at a time: re-run it forward recording acc
     // at the design points, then its transposed steps in reverse
+    bool first = true;  // the sweep's first transposed step has no gather to fold in
     for (long long seg = nseg - 1; seg >= 0; --seg) {
         const long long t0 = seg * K, t1 = std::min(N, t0 + K);
         restore(seg);
@@ -1712,10 +1713,10 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
         for (long long n = t0; n < t1; ++n) ck(launch_one<real>(sim), "step launch");
         for (int q = 0; q < ni; ++q) dv[q].rec_acc = nullptr, dv[q].rec_len = 0;
         upload_table<real>(sim);
-        for (long long n = t1 - 1; n >= t0; --n)
+        for (long long n = t1 - 1; n >= t0; --n, first = false)
             for (int q = 0; q < ni; ++q) {
                 A[q].rec_t0 = t0;
-                ck(launch_adjoint_step<real>(A[q], n, st), "adjoint step");
+                ck(launch_adjoint_step<real>(A[q], n, first, st), "adjoint step");
                 ck(launch_objective<real>(dv[q], sim->cur, d_cells[q], objs[q].n_cells, objs[q].comp_mask,
                                           objs[q].frequency, d_D[q], n, false, A[q].eb, st),
                    "adjoint source");

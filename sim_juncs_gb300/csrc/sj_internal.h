@@ -259,8 +259,10 @@ struct AdjDev {
     long long rec_t0;
     double* g;                  // dF/d(inverse eps) at the design points [d][3]
 };
+// Adjoint step n: the E update's transpose (first = false: with step n+1's
+// gather into dF/dE folded in) and the H update's.
 template <typename real>
-cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, cudaStream_t s);
+cudaError_t launch_adjoint_step(const AdjDev<real>& a, long long n, bool first, cudaStream_t s);
 // Objective DFT of one instance: D[q][c] += dt E_c^n(cell q) e^{i 2 pi f n dt}
 // (sample = true, from buffer cur) or dF/dE^n source into eb (sample = false).
 template <typename real>
