@@ -464,7 +464,8 @@ int sj_divergence(const sj_sim* sim, int64_t* step, int32_t* inst, int32_t* moni
    the interval (each segment is re-run once).  checkpoint_every <= 0 or
    >= N keeps one segment: two state copies and the bracket of all N steps,
    the least memory whenever the design region is small.  An interval whose
-   copies do not fit the free device memory fails with SJ_E_NOMEM. */
+   copies do not fit the free device memory fails with SJ_E_NOMEM; an
+   instance of 2^31 voxels or more (row pitch included) with SJ_E_INVALID. */
 typedef struct {
     int32_t lo[3];              /* first voxel of the design box */
     int32_t n[3];               /* extent in voxels */

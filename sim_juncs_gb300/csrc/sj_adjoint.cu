@@ -58,6 +58,8 @@ __device__ __forceinline__ long long design_index(const InstDev<real>& I, int i,
 // -1 neighbours).  Every load of the voxel goes out first (eb, t3 and t4, the E-side
 // psi adjoints of its slab axes, the polarisation adjoints of the poles its
 // material has: pmask), then the three components are formed in turn.
+// Offsets within the instance are 32-bit (sj_adjoint_gradient admits grids
+// of fewer than 2^31 voxels), and each slab axis' profile is read once.
 #ifndef SJ_ADJ_E_MINB
 #define SJ_ADJ_E_MINB 3
 #endif
@@ -66,17 +68,28 @@ __global__ void __launch_bounds__(AX * AY, SJ_ADJ_E_MINB) k_adj_e(const __grid_c
     const InstDev<real>& I = A.I;
     const int i = blockIdx.x * AX + threadIdx.x, j = blockIdx.y * AY + threadIdx.y, k = blockIdx.z;
     if (i >= I.nx || j >= I.ny) return;
-    const long long o = (long long)k * I.plane + (long long)j * I.px + i;
+    const unsigned vol = (unsigned)I.vol;
+    const unsigned st[3] = {1u, (unsigned)I.px, (unsigned)I.plane};
+    const unsigned o = (unsigned)k * st[2] + (unsigned)j * st[1] + (unsigned)i;
     const int idx[3] = {i, j, k};
     const int cb = I.combo[o];
     const real* cf = I.coef + cb * I.ncoef;
     const unsigned mask = I.pmask[cb];
-    const long long di =
-        mask ? ((long long)(k - I.dlo[2]) * I.dn[1] + (j - I.dlo[1])) * I.dn[0] + (i - I.dlo[0]) : 0;
+    const unsigned di = mask ? ((unsigned)(k - I.dlo[2]) * (unsigned)I.dn[1] + (unsigned)(j - I.dlo[1])) *
+                                       (unsigned)I.dn[0] + (unsigned)(i - I.dlo[0])
+                             : 0u;
+    const size_t dvol = (size_t)I.dvol;
     const long long d = design_index(I, i, j, k);
     const long long nd = (long long)I.des_n[0] * I.des_n[1] * I.des_n[2];
     const bool sl[3] = {in_slab(I, 0, i), in_slab(I, 1, j), in_slab(I, 2, k)};
-    real ebo[3], q1[3], q2[3], b0[3], b1[3], c0[3], c1[3];
+    // the CPML profile (integer points) of each slab axis at the voxel
+    real pb_[3], pc_[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        pb_[a] = sl[a] ? prof_at(I, a, idx[a], 0) : real(0);
+        pc_[a] = sl[a] ? prof_at(I, a, idx[a], 1) : real(0);
+    }
+    real ebo[3], q1[3], q2[3];
     real g3[3], g4[3], m3[3], m4[3];  // GATHER: t3, t4 here and at the -1 neighbours
     int pa[3], pz[3];
     real pa0[3], pa1[3], pz0[3], pz1[3];
@@ -86,23 +99,22 @@ __global__ void __launch_bounds__(AX * AY, SJ_ADJ_E_MINB) k_adj_e(const __grid_c
         const int a1 = (ca + 1) % 3, a2 = (ca + 2) % 3;
         const int s1 = ca > a1 ? ca - 1 : ca, s2 = ca > a2 ? ca - 1 : ca;
         ebo[ca] = A.eb[ca][o];
-        q1[ca] = sl[a1] ? A.psEb[a1][(long long)s1 * I.vol + o] : real(0);
-        q2[ca] = sl[a2] ? A.psEb[a2][(long long)s2 * I.vol + o] : real(0);
-        b0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 0) : real(0), c0[ca] = sl[a1] ? prof_at(I, a1, idx[a1], 1) : real(0);
-        b1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 0) : real(0), c1[ca] = sl[a2] ? prof_at(I, a2, idx[a2], 1) : real(0);
+        q1[ca] = sl[a1] ? A.psEb[a1][(unsigned)s1 * vol + o] : real(0);
+        q2[ca] = sl[a2] ? A.psEb[a2][(unsigned)s2 * vol + o] : real(0);
         if (GATHER) {
             g3[ca] = A.t3[ca][o], g4[ca] = A.t4[ca][o];
-            m3[ca] = idx[a1] > 0 ? A.t3[ca][o - stride_of(I, a1)] : real(0);
-            m4[ca] = idx[a2] > 0 ? A.t4[ca][o - stride_of(I, a2)] : real(0);
+            m3[ca] = idx[a1] > 0 ? A.t3[ca][o - st[a1]] : real(0);
+            m4[ca] = idx[a2] > 0 ? A.t4[ca][o - st[a2]] : real(0);
         }
         const unsigned m = (mask >> (8 * ca)) & 255u, m2 = m & (m - 1);
         pa[ca] = m ? __ffs(m) - 1 : -1;
         pz[ca] = m2 ? __ffs(m2) - 1 : -1;
         rest[ca] = m2 & (m2 - 1);
-        const long long x0 = ((long long)(pa[ca] * 2) * 3 + ca) * I.dvol + di;
-        const long long x1 = ((long long)(pz[ca] * 2) * 3 + ca) * I.dvol + di;
-        pa0[ca] = m ? A.pb[x0] : real(0), pa1[ca] = m ? A.pb[x0 + 3 * I.dvol] : real(0);
-        pz0[ca] = m2 ? A.pb[x1] : real(0), pz1[ca] = m2 ? A.pb[x1 + 3 * I.dvol] : real(0);
+        // a pole's dF/dP^{n+1} at level 0 of its rows, dF/dP^n three rows on
+        const real* P0 = A.pb + (size_t)(max(pa[ca], 0) * 6 + ca) * dvol + di;
+        const real* P1 = A.pb + (size_t)(max(pz[ca], 0) * 6 + ca) * dvol + di;
+        pa0[ca] = m ? P0[0] : real(0), pa1[ca] = m ? P0[3 * dvol] : real(0);
+        pz0[ca] = m2 ? P1[0] : real(0), pz1[ca] = m2 ? P1[3 * dvol] : real(0);
     }
     if (GATHER) {
         // dF/dE^{n+1} += what the H update's differences of step n+1 read here
@@ -127,8 +139,8 @@ __global__ void __launch_bounds__(AX * AY, SJ_ADJ_E_MINB) k_adj_e(const __grid_c
         real ein = ebo[ca];
         // one pole's ADE transpose: (dF/dP^{n+1}, dF/dP^n) -> (dF/dP^n, dF/dP^{n-1})
         auto pole = [&](int p, real q0v, real q1v) {
-            real* p0 = A.pb + ((long long)(p * 2 + 0) * 3 + ca) * I.dvol + di;
-            real* p1 = A.pb + ((long long)(p * 2 + 1) * 3 + ca) * I.dvol + di;
+            real* p0 = A.pb + (size_t)(p * 6 + ca) * dvol + di;
+            real* p1 = p0 + 3 * dvol;
             const real pnb = q0v - ab;                    // dF/dP^{n+1}
             const real pn = q1v + ab + I.A[p] * pnb;      // dF/dP^n
             *p1 = I.B[p] * pnb;                           // dF/dP^{n-1}
@@ -139,21 +151,21 @@ __global__ void __launch_bounds__(AX * AY, SJ_ADJ_E_MINB) k_adj_e(const __grid_c
         if (pz[ca] >= 0) pole(pz[ca], pz0[ca], pz1[ca]);
         for (unsigned m = rest[ca]; m; m &= m - 1) {
             const int p = __ffs(m) - 1;
-            const long long x = ((long long)(p * 2) * 3 + ca) * I.dvol + di;
-            pole(p, A.pb[x], A.pb[x + 3 * I.dvol]);
+            const real* x = A.pb + (size_t)(p * 6 + ca) * dvol + di;
+            pole(p, x[0], x[3 * dvol]);
         }
         A.eb[ca][o] = ein;
         const real cv = I.S * ab;  // adjoint of the curl
         real t1 = cv, t2 = -cv;
         if (sl[a1]) {
             const real t = q1[ca] + cv;
-            t1 = cv + c0[ca] * t;
-            A.psEb[a1][(long long)s1 * I.vol + o] = b0[ca] * t;
+            t1 = cv + pc_[a1] * t;
+            A.psEb[a1][(unsigned)s1 * vol + o] = pb_[a1] * t;
         }
         if (sl[a2]) {
             const real t = q2[ca] - cv;
-            t2 = -cv + c1[ca] * t;
-            A.psEb[a2][(long long)s2 * I.vol + o] = b1[ca] * t;
+            t2 = -cv + pc_[a2] * t;
+            A.psEb[a2][(unsigned)s2 * vol + o] = pb_[a2] * t;
         }
         A.t1[ca][o] = t1;  // adjoint of H_a2(o) - H_a2(o - e_a1)
         A.t2[ca][o] = t2;  // adjoint of H_a1(o) - H_a1(o - e_a2)

@@ -1567,6 +1567,9 @@ void adjoint_t(sj_sim* sim, const sj_objective_desc* objs, long long N, long lon
         fail(SJ_E_RANGE, "d_obj_d_eps too small for the design voxels");
     if (!backward) K = N;  // the final state is the only one kept
     if (sim->schedule == SJ_SCHED_TMA) fail(SJ_E_INVALID, "the adjoint steps with the fused or split schedule");
+    for (int q = 0; q < ni; ++q)  // the adjoint kernels address an instance with 32-bit offsets
+        if ((unsigned long long)dv[q].vol >= (1ull << 31))
+            fail(SJ_E_INVALID, "the adjoint takes grids of fewer than 2^31 voxels (row pitch included)");
     ensure_capacity<real>(sim, N);
     prepare_schedule<real>(sim);
     cudaStream_t st = sim->stream;
