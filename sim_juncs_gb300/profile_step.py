@@ -36,22 +36,29 @@ def instances(name):
         return [configs.bowtie_instance()]
     if name == "junction64":
         return [configs.junction_instance()]
-    if name.startswith("inverse"):
-        return [configs.inverse_design_case(d)[0] for d in range(int(name[7:]))]
+    if _inverse_count(name):
+        return [configs.inverse_design_case(d)[0] for d in range(_inverse_count(name))]
     raise SystemExit(f"unknown workload {name!r}")
+
+
+def _inverse_count(name):
+    """N of an inverseN workload name (1..16), else 0."""
+    if name.startswith("inverse") and name[7:].isdigit() and 1 <= int(name[7:]) <= 16:
+        return int(name[7:])
+    return 0
 
 
 def objectives(name):
     """The objectives of a workload's instances (inverseN only)."""
-    if name.startswith("inverse"):
-        return [configs.inverse_design_case(d)[2] for d in range(int(name[7:]))]
+    if _inverse_count(name):
+        return [configs.inverse_design_case(d)[2] for d in range(_inverse_count(name))]
     raise SystemExit(f"{name!r} has no objectives")
 
 
 def designs(name):
     """The design regions a workload's instances carry (instance, Design)."""
-    if name.startswith("inverse"):
-        return [(d, configs.inverse_design_case(d)[1]) for d in range(int(name[7:]))]
+    if _inverse_count(name):
+        return [(d, configs.inverse_design_case(d)[1]) for d in range(_inverse_count(name))]
     return []
 
 
