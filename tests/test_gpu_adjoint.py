@@ -234,3 +234,19 @@ def test_gpu_gradient_matches_central_differences(lib, central_differences, prec
     assert scale > 0
     err = float(np.max(np.abs(got - fd))) / scale
     assert err <= tol, (precision, schedule, err)
+
+
+def test_three_pole_adjoint_matches_oracle(lib, oracle_lib):
+    # every gold E point with three polarisation adjoints: past the two per
+    # point the E transpose loads up front
+    from test_gpu_configs import three_pole_gold
+    inst, des, obj = setup()
+    inst = three_pole_gold(inst)
+    o = OracleFields(inst)
+    o.set_design(des)
+    Fo, go = o.adjoint(obj, N_STEPS)
+    f = Fields(inst, "f64")
+    f.set_design(des)
+    F, g = f.adjoint_gradient(obj, N_STEPS, checkpoint_every=50)
+    assert F[0] == pytest.approx(Fo, rel=1e-10)
+    assert rel(g[0], go) <= 1e-8

@@ -139,3 +139,22 @@ def test_reference_rounding_65_cubed_f64_matches_oracle(lib, oracle_lib):
     inst = junction_instance(n=g.nx, res=res)
     f = check_against_oracle(inst, 2000, (1, 400))
     assert gold_field(f, inst) > 0
+
+
+def three_pole_gold(inst):
+    """The scene's gold with a third (Lorentz) pole: every gold E point then
+    carries three polarisations, the case past the polarisation kernels' two
+    poles per point loaded up front."""
+    from sim_juncs_gb300.configs import AU
+    from sim_juncs_gb300.spec import Susceptibility
+    inst.material.regions[0].susceptibilities = list(AU) + [Susceptibility(0.8, 0.1, 0.3, drude=False)]
+    return inst
+
+
+def test_three_pole_gold_f64_matches_oracle(lib, oracle_lib):
+    inst = three_pole_gold(early_pulse(junction_instance(n=64, res=20.0)))
+    f = check_against_oracle(inst, 200, (1, 100))
+    assert gold_field(f, inst) > 0
+    g = Fields(inst, "f32")
+    g.step(200)
+    assert rel(g.monitors(), f.monitors()) <= TOL32
